@@ -1,0 +1,226 @@
+/*
+ * wcfd.h -- C ABI of libwcfd.so, the GB300 (sm_103a) kernels of the collocated
+ * finite-volume SIMPLE/PISO step.
+ *
+ * Conventions
+ *   - Every pointer in the structs below is a DEVICE pointer owned by the caller
+ *     (in the Python layer: torch tensors).  The library allocates no device memory
+ *     on any path declared here except where an entry point says so.
+ *   - Every call is asynchronous on the given cudaStream_t (passed as void*; NULL =
+ *     legacy default stream) and returns an int status (WCFD_OK = 0).
+ *   - Solver outcomes (iteration count, final residual, breakdown, barrier timeout)
+ *     are written to a caller-owned device wcfd_solve_stats record; reading it is
+ *     the caller's synchronisation point.
+ *   - Floating point: fields, geometry and matrices are fp32; Krylov dot products and
+ *     residual norms are accumulated in fp64.
+ *   - No exception crosses the ABI.  One host thread per case at a time.
+ *
+ * The reference (warp_cfd, NVIDIA Warp) has no C ABI: its operator API is the Python
+ * package.  Each entry point below names the reference function/kernel it replaces
+ * (path:line within the warp_cfd project).
+ */
+#ifndef WCFD_H
+#define WCFD_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+#define WCFD_OK                  0
+#define WCFD_ERR_ARGUMENT        1  /* null pointer, bad size or flag              */
+#define WCFD_ERR_CUDA            2  /* a CUDA runtime call failed (see last_error)  */
+#define WCFD_KRYLOV_BREAKDOWN    3  /* a Krylov denominator became exactly zero     */
+#define WCFD_NOT_CONVERGED       4  /* maxiter reached (informational, as in warp)  */
+#define WCFD_BARRIER_TIMEOUT     5  /* a grid barrier wait gave up (bounded spin)   */
+#define WCFD_ERR_TOO_LARGE       6  /* size beyond what the entry point supports    */
+
+/* field mask bits: u, v, w, p (columns 0..3 of cell_values) */
+#define WCFD_U 1u
+#define WCFD_V 2u
+#define WCFD_W 4u
+#define WCFD_P 8u
+#define WCFD_ALL 15u
+
+/* ------------------------------------------------------------------ mesh (SoA)
+ * K faces, C cells, B boundary faces, F local face slots per cell (uniform cell type),
+ * W = max internal faces of any cell (width of the slot-major off-diagonal storage).
+ * Face ids and their order are the reference's (unique sorted node tuples).
+ */
+typedef struct wcfd_mesh {
+    int32_t n_cells;          /* C */
+    int32_t n_faces;          /* K */
+    int32_t n_bfaces;         /* B */
+    int32_t faces_per_cell;   /* F (<= 6) */
+    int32_t ell_width;        /* W (<= F) */
+    int32_t pad_;
+    const int32_t* face_owner;    /* [K]   owner cell (lower id)                      */
+    const int32_t* face_nbr;      /* [K]   neighbour cell, -1 on boundary faces       */
+    const int32_t* face_brow;     /* [K]   row in the boundary tables, -1 internal    */
+    const float*   face_interp;   /* [K*4] skew vector r_f - (psi r_P + (1-psi) r_N), psi */
+    const float*   face_normal;   /* [K*4] owner's outward unit normal, area          */
+    const float*   face_gdiff;    /* [K]   area/|d| (internal; x|n1| when corrected), area/|r_Pf| (boundary) */
+    const float*   face_rpf;      /* [K]   |r_P->f| (owner centroid to face centroid) */
+    const float*   cell_slot;     /* [F*C*4] slot-major: A n_cf / V (3), bits of the signed face id
+                                     (k for the owner side, ~k for the neighbour side) */
+    const float*   cell_volume;   /* [C]                                               */
+    const int32_t* ell_col;       /* [W*C] slot-major neighbour column; padding = own row */
+    const int32_t* boundary_face; /* [B]   face id of each boundary row               */
+} wcfd_mesh;
+
+/* boundary tables, one row per boundary face, columns u,v,w,p */
+typedef struct wcfd_bc {
+    const uint8_t* type;   /* [B*4] 1 = fixed value, 2 = fixed normal gradient */
+    const float*   value;  /* [B*4]                                             */
+} wcfd_bc;
+
+/* the model's field state (the reference's FVM arrays, model.py:167-171) */
+typedef struct wcfd_state {
+    float* cell_values;     /* [C*4]   u,v,w,p                      */
+    float* cell_gradients;  /* [C*4*3]                               */
+    float* face_values;     /* [K*4]                                 */
+    float* face_gradients;  /* [K*4]   only boundary rows are used   */
+    float* mass_fluxes;     /* [K]                                   */
+} wcfd_state;
+
+/* scalar or 3-component system on the mesh pattern: diagonal + W off-diagonals per row
+ * (slot-major, column = mesh.ell_col).  For the momentum system the off-diagonals are
+ * shared by u, v, w and diag/rhs are interleaved [C*3] (row 3c+o, as the reference's
+ * interleaved BSR rows D*i+o, equation_kernels.py:10-38). */
+typedef struct wcfd_system {
+    float* diag;     /* [C] or [C*3] */
+    float* off;      /* [W*C]        */
+    float* rhs;      /* [C] or [C*3] */
+    int32_t ncomp;   /* 1 or 3       */
+    int32_t pad_;
+} wcfd_system;
+
+/* Krylov workspace (caller-allocated, see wcfd_krylov_workspace_floats) */
+typedef struct wcfd_krylov_ws {
+    float*    vec;        /* wcfd_krylov_workspace_floats(C, ncomp) floats        */
+    double*   partials;   /* 8 * WCFD_MAX_BLOCKS doubles                          */
+    double*   results;    /* 8 doubles                                            */
+    uint32_t* barrier;    /* 4 words: count, generation, error; the call zeroes them */
+} wcfd_krylov_ws;
+
+#define WCFD_MAX_BLOCKS 2048
+
+typedef struct wcfd_solve_stats {
+    int32_t iterations;
+    int32_t status;       /* WCFD_OK, WCFD_NOT_CONVERGED, WCFD_KRYLOV_BREAKDOWN, WCFD_BARRIER_TIMEOUT */
+    double  residual;     /* ||b - A x||_2 at exit (fp64)                         */
+} wcfd_solve_stats;
+
+/* per-case scalars of one SIMPLE iteration / PISO step */
+typedef struct wcfd_params {
+    float   nu;             /* kinematic viscosity mu/rho (incompressible.py:89) */
+    float   rho;            /* density                                           */
+    float   u_relax;        /* implicit momentum relaxation; <= 0 = none          */
+    float   p_relax;        /* explicit p relaxation; <= 0 = replace              */
+    float   dt;             /* PISO time step                                     */
+    float   ref_value;      /* reference pressure value                           */
+    int32_t ref_cell;       /* reference pressure cell, -1 = none                 */
+    int32_t steady;         /* 1 = SIMPLE (steady), 0 = PISO (ddt term)           */
+    int32_t n_inner;        /* pressure correctors                                */
+    int32_t n_ortho;        /* non-orthogonal correctors                          */
+    int32_t maxiter;        /* Krylov cap (500 in the reference)                  */
+    int32_t skew;           /* skew correction in face interpolation (1)          */
+    double  atol_u;         /* momentum BiCGSTAB absolute tolerance               */
+    double  atol_p;         /* pressure CG absolute tolerance                     */
+} wcfd_params;
+
+/* a full case: everything one SIMPLE iteration touches */
+typedef struct wcfd_case {
+    wcfd_mesh      mesh;
+    wcfd_bc        bc;
+    wcfd_state     state;
+    wcfd_system    mom;        /* ncomp 3 */
+    wcfd_system    pres;       /* ncomp 1 */
+    float*         hbya;       /* [C*3] HbyA (incompressible.py:43), momentum x0/out */
+    float*         p_x;        /* [C]   pressure solution / warm start (equation.py:68-71) */
+    float*         rua;        /* [C]   rUA = V/(a_P rho)                             */
+    float*         rua_faces;  /* [K]                                                */
+    float*         div;        /* [C]   div of the mass flux                          */
+    wcfd_krylov_ws ws_u;       /* momentum workspace (ncomp 3)                        */
+    wcfd_krylov_ws ws_p;       /* pressure workspace (ncomp 1)                        */
+    wcfd_solve_stats* stats;   /* [2]: [0] momentum, [1] pressure (last corrector)    */
+    wcfd_params    prm;
+} wcfd_case;
+
+/* ------------------------------------------------------------------ info */
+int         wcfd_version(void);
+const char* wcfd_last_error(void);
+/* floats of wcfd_krylov_ws.vec needed for a C-row system with ncomp components */
+int64_t     wcfd_krylov_workspace_floats(int32_t n_cells, int32_t ncomp);
+
+/* ------------------------------------------------------------------ field operators */
+/* FVM.set_boundary_conditions (model.py:206-208, conditions.py:5-19): fixed values onto
+ * face_values, fixed gradients onto face_gradients, for every field of every boundary face. */
+int wcfd_set_boundary_conditions(const wcfd_mesh* m, wcfd_bc bc, wcfd_state s, void* stream);
+
+/* FVM.face_interpolation (model.py:210-229; interpolation_kernels.py:5-54,
+ * interpolation_functions.py:5-28, skewness_functions.py:6-19) for the fields in `mask`:
+ * linear, or upwind on the current mass flux when `upwind`, plus the skew correction when
+ * `skew`, on internal faces; phi_P + |r_Pf| g on fixed-gradient boundary faces. */
+int wcfd_face_interpolation(const wcfd_mesh* m, wcfd_bc bc, wcfd_state s, uint32_t mask,
+                            int32_t skew, int32_t upwind, void* stream);
+
+/* The three above fused in one face pass: flags bit0 = set boundary conditions first,
+ * bit1 = mass flux from the new face values, bit2 = skew correction, bit3 = upwind. */
+int wcfd_face_pass_flags(const wcfd_mesh* m, wcfd_bc bc, wcfd_state s, uint32_t mask,
+                         uint32_t flags, void* stream);
+
+/* FVM.calculate_mass_flux (model.py:264-266, model_kernels.py:45-60):
+ * mdot = (u_f, v_f, w_f) . n_owner A. */
+int wcfd_calculate_mass_flux(const wcfd_mesh* m, wcfd_state s, void* stream);
+
+/* FVM.calculate_gradients (model.py:232-239, model_kernels.py:71-90): Green-Gauss gradient
+ * of the fields in `mask`; every other field's gradient is set to zero, as the reference's
+ * cell_gradients.zero_() does.  Atomic-free (one thread per cell). */
+int wcfd_calculate_gradients(const wcfd_mesh* m, wcfd_state s, uint32_t mask, void* stream);
+
+/* FVM.divFlux (model.py:269-275, model_kernels.py:26-34): div[c] = sum of +-mdot. */
+int wcfd_div_flux(const wcfd_mesh* m, const float* mass_fluxes, float* div, void* stream);
+
+/* interpolate_cell_value_to_face (solver_kernels.py:21-36): psi-weighted for internal
+ * faces, owner value on boundary faces. */
+int wcfd_cell_to_face(const wcfd_mesh* m, const float* cell, float* face, void* stream);
+
+/* ------------------------------------------------------------------ assembly */
+/* Momentum system of one SIMPLE iteration / PISO predictor, in one cell-parallel pass:
+ * ConvectionTerm upwind (convection.py:43-91), DiffusionTerm with scalar nu
+ * (diffusion.py:113-198), DdtTerm when !steady (ddt.py:24-32), explicit -grad(p) V / rho
+ * (grad.py:20-29, incompressible.py:107), Equation.form_system (equation.py:99-125,
+ * equation_kernels.py:52-122), implicit relaxation (equation_kernels.py:128-152) and
+ * rUA = V/(a_P[u] rho) (solver_kernels.py:6-16).  No atomics: each cell writes its row. */
+int wcfd_assemble_momentum(const wcfd_case* c, void* stream);
+
+/* Pressure system: DiffusionTerm('p', nu = rUA_f) + div(HbyA) on the RHS + reference
+ * row (incompressible.py:132-140, equation_kernels.py:155-175). */
+int wcfd_assemble_pressure(const wcfd_case* c, void* stream);
+
+/* y = A x on the mesh pattern (warp.sparse.bsr_mv; model.py:287). */
+int wcfd_spmv(const wcfd_mesh* m, wcfd_system A, const float* x, float* y, void* stream);
+
+/* ------------------------------------------------------------------ Krylov solves
+ * Persistent cooperative kernels (one launch per solve, bounded grid barriers, fp64
+ * reductions).  Replace warp.optim.linear.cg / bicgstab with the diagonal preconditioner
+ * (Equation.solve_Axb, equation.py:195-200).  Stop: ||r||_2 <= atol before an iteration,
+ * or maxiter. */
+int wcfd_cg(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, double atol,
+            int32_t maxiter, wcfd_solve_stats* stats, void* stream);
+int wcfd_bicgstab(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, double atol,
+                  int32_t maxiter, wcfd_solve_stats* stats, void* stream);
+
+/* ------------------------------------------------------------------ fused steps */
+/* One steady SIMPLE outer iteration (incompressible.py:95-156 with steady_state=True),
+ * or one PISO time step (NUM_OUTER_LOOPS = 1, steady_state=False), as a fixed sequence of
+ * fused kernels on `stream`; capturable in a CUDA graph. */
+int wcfd_simple_iteration(const wcfd_case* c, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WCFD_H */

@@ -1,0 +1,150 @@
+"""IncompressibleSolver: SIMPLE / PISO driver with the API of
+warp_cfd/FV/implicit_Solvers/incompressible.py:10-172.
+
+One outer iteration (or PISO time step) is one call of ``wcfd_simple_iteration``, a fixed
+sequence of fused kernels and two persistent Krylov launches on the current stream; with
+``use_cuda_graph`` the sequence is captured once and replayed.  Solver outcomes stay on
+the device until a convergence check reads them.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+
+import numpy as np
+import torch
+
+from ... import _lib
+from ..model import FVM, _stream
+from ..terms import ConvectionTerm, DdtTerm, DiffusionTerm, Equation, GradTerm
+
+STATS_DTYPE = np.dtype([("iterations", "<i4"), ("status", "<i4"), ("residual", "<f8")])
+
+
+class IncompressibleSolver:
+    def __init__(self, model: FVM, u_relaxation_factor=None, p_relaxation_factor=None, correction=False,
+                 steady_state=True) -> None:
+        if not model.finalized:
+            raise ValueError("Please call method model.finalize() before passing model in to solver")
+        self.model = model
+        self.float_dtype = model.float_dtype
+        velocity_vars = ["u", "v", "w"]
+        self.steady_state = steady_state
+        self.correction = correction
+        if not steady_state:
+            self.ddt = DdtTerm(model, velocity_vars)
+        self.convection = ConvectionTerm(model, velocity_vars, "upwind")
+        self.diffusion = DiffusionTerm(model, velocity_vars, correction=correction)
+        self.grad_P = GradTerm(model, "p")
+        self.vel_equation = Equation(model, fields=velocity_vars)
+        self.p_correction_diffusion = DiffusionTerm(model, "p", correction=correction)
+        self.p_corr_equation = Equation(model, fields="p", solver="cg")
+        self.p_relaxation_factor = p_relaxation_factor
+        self.u_relaxation_factor = u_relaxation_factor
+        self.material = model.material
+        C, K, dev = model.num_cells, model.num_faces, model.device
+        f32 = dict(dtype=torch.float32, device=dev)
+        self.HbyA = self.vel_equation.x          # (3C) interleaved, the momentum x0/out
+        self.rUA = torch.zeros(C, **f32)
+        self.rUA_faces = torch.zeros(K, **f32)
+        self.div_u = torch.zeros(C, **f32)
+        self.vel_correction = torch.zeros(C * 3, **f32)
+        self.stats = torch.zeros(2 * STATS_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+        self.set_time_stepping(1, 1.0)
+        self.NUM_ORTHOGONAL_CORRECTORS = 1
+        self.NUM_OUTER_LOOPS = 1
+        self.NUM_INNER_LOOPS = 1
+        self.steps_done = 0
+        self.verbose = True
+        self._graph = None
+        self._graph_key = None
+        self._mesh_t = model.mesh_struct(correction=correction)
+
+    def set_time_stepping(self, MAX_TIME_STEPS, dt, automatic=False, CFL_Max=1.0):
+        if automatic is not False:
+            raise NotImplementedError("automatic time stepping not yet implemented")
+        self.MAX_TIME_STEPS = MAX_TIME_STEPS
+        self.dt = dt
+
+    def set_iterations(self, NUM_OUTER_LOOPS, NUM_INNER_LOOPS, NUM_ORTHOGONAL_CORRECTORS):
+        self.NUM_OUTER_LOOPS = NUM_OUTER_LOOPS
+        self.NUM_INNER_LOOPS = NUM_INNER_LOOPS
+        self.NUM_ORTHOGONAL_CORRECTORS = NUM_ORTHOGONAL_CORRECTORS
+
+    # ------------------------------------------------------------------ case struct
+    def params(self) -> _lib.Params_t:
+        m = self.model
+        rho = float(self.material.density)
+        nu = float(self.material.viscosity) / rho
+        steady = bool(self.steady_state)
+        ur = self.u_relaxation_factor if (steady and self.u_relaxation_factor is not None) else 0.0
+        pr = self.p_relaxation_factor if (steady and self.p_relaxation_factor is not None) else 0.0
+        ref = m.reference_pressure_cell_id
+        return _lib.Params_t(nu, rho, float(ur), float(pr), float(self.dt), float(m.reference_pressure),
+                             -1 if ref is None else int(ref), int(steady), int(self.NUM_INNER_LOOPS),
+                             int(self.NUM_ORTHOGONAL_CORRECTORS), int(self.vel_equation.max_iter),
+                             int(bool(m.skew_correction)), float(self.vel_equation.tol),
+                             float(self.p_corr_equation.tol))
+
+    def case_struct(self) -> _lib.Case_t:
+        m = self.model
+        ve, pe = self.vel_equation, self.p_corr_equation
+        return _lib.Case_t(self._mesh_t, m.bc_struct(), m.state_struct(), ve.system_struct(), pe.system_struct(),
+                           self.HbyA.data_ptr(), pe.x.data_ptr(), self.rUA.data_ptr(), self.rUA_faces.data_ptr(),
+                           self.div_u.data_ptr(), ve.workspace_struct(), pe.workspace_struct(),
+                           self.stats.data_ptr(), self.params())
+
+    # ------------------------------------------------------------------ stepping
+    def step(self):
+        """One SIMPLE outer iteration or one PISO time step on the current stream."""
+        case = self.case_struct()
+        _lib.call("wcfd_simple_iteration", ct.byref(case), _stream())
+
+    def solve_stats(self):
+        """(momentum, pressure) Krylov outcomes of the last step: iterations, status, residual."""
+        raw = np.frombuffer(self.stats.cpu().numpy().tobytes(), dtype=STATS_DTYPE)
+        return [dict(iterations=int(r["iterations"]), status=_lib.STATUS_NAMES.get(int(r["status"]), "?"),
+                     residual=float(r["residual"])) for r in raw]
+
+    def momentum_residual_operator(self):
+        return self.vel_equation.apply
+
+    def run(self, steps_per_check=10, use_cuda_graph=False):
+        """incompressible.py:72-172 (the convergence check never stops the loop, as there)."""
+        nsteps = self.NUM_OUTER_LOOPS if self.steady_state else self.MAX_TIME_STEPS
+        for nt in range(self.MAX_TIME_STEPS if not self.steady_state else 1):
+            for n_outer in range(self.NUM_OUTER_LOOPS if self.steady_state else 1):
+                if use_cuda_graph:
+                    self._graph_step_counted()
+                else:
+                    self.step()
+                steps = n_outer if self.steady_state else nt
+                if steps_per_check and steps % steps_per_check == 0:
+                    self.report(steps)
+        if self.verbose:
+            print(f"MAX ITERATIONS OF {nsteps} REACHED. Terminating")
+        return self.report(nsteps)
+
+    def _graph_step_counted(self):
+        if self._graph is None or bytes(self.case_struct()) != self._graph_key:
+            # first call captures; the capture itself does not execute, so run one eager step
+            key = bytes(self.case_struct())
+            self.step()
+            torch.cuda.synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                self.step()
+            self._graph, self._graph_key = g, key
+        else:
+            self._graph.replay()
+
+    def report(self, steps):
+        ve = self.vel_equation
+        st = self.solve_stats()
+        vc = self.model.cell_gradients[:, 3, :].reshape(-1) * self.rUA.repeat_interleave(3)
+        conv, converged = self.model.check_convergence(ve.apply, self.HbyA, ve.rhs, self.div_u, vc,
+                                                       self.p_corr_equation.x)
+        if self.verbose:
+            print(f"step iter: {steps}")
+            print(f"Outer loop Linear Solve {st[0]} Inner loop solve {st[1]}:")
+            print({k: (v if isinstance(v, float) else (round(v[0], 9), v[1])) for k, v in conv.items()})
+        return conv, converged

@@ -1,0 +1,138 @@
+"""Equation: the fixed-pattern linear system of one or three fields
+(warp_cfd/FV/terms/equation.py:10-204).
+
+Storage (per mesh, fixed for the run): ``diag`` (C*n, interleaved rows n*c + o as the
+reference's BSR rows D*i+o), ``off`` (W x C, slot-major; shared by the n components
+because the momentum off-diagonals do not depend on the component), ``rhs`` (C*n),
+solution ``x`` (C*n).  ``matrix`` / ``dense`` export the same operator in CSR form.
+``solve_Axb`` runs the persistent Krylov kernel: BiCGSTAB for n = 3 (the reference's
+default solver, equation.py:11) and CG for n = 1 when ``solver='cg'``
+(incompressible.py:32), Jacobi-preconditioned, atol 1e-5 (fp32), maxiter 500
+(equation.py:35-39).
+"""
+from __future__ import annotations
+
+import ctypes as ct
+
+import numpy as np
+import torch
+
+from ... import _lib
+from ..field import Field
+
+
+class Equation:
+    def __init__(self, fvm, fields, solver="bicgstab") -> None:
+        if isinstance(fields, str):
+            fields = [fields]
+        if all(f in fvm.output_variables for f in fields):
+            self.fields = [fvm.fields[f] for f in fields]
+            self.global_output_indices = [f.index for f in self.fields]
+        else:
+            self.fields = [Field(f) for f in fields]
+            self.global_output_indices = None
+        self.num_outputs = len(fields)
+        if self.num_outputs not in (1, 3):
+            raise NotImplementedError("systems of 1 field (scalar) or 3 fields (velocity) are supported")
+        solver = getattr(solver, "__name__", solver)
+        if solver not in ("cg", "bicgstab"):
+            raise ValueError("solver must be 'cg' or 'bicgstab'")
+        if solver == "cg" and self.num_outputs != 1:
+            raise NotImplementedError("cg is provided for scalar systems")
+        if solver == "bicgstab" and self.num_outputs != 3:
+            solver = "cg"
+        self.linear_solver = solver
+        self.fvm = fvm
+        self.max_iter = 500
+        self.tol = 1.0e-5
+        C = fvm.num_cells
+        n = self.num_outputs
+        W = fvm._geo["ell_width"]
+        dev = fvm.device
+        f32 = dict(dtype=torch.float32, device=dev)
+        self.sparse_rows = C * n
+        self.diag = torch.zeros(C * n, **f32)
+        self.off = torch.zeros(max(W, 1) * C, **f32)
+        self.rhs = torch.zeros(C * n, **f32)
+        self._x = torch.zeros(C * n, **f32)
+        lib = _lib.load()
+        nws = int(lib.wcfd_krylov_workspace_floats(C, n))
+        self.ws_vec = torch.zeros(nws, **f32)
+        self.ws_partials = torch.zeros(8 * _lib.MAX_BLOCKS, dtype=torch.float64, device=dev)
+        self.ws_results = torch.zeros(8, dtype=torch.float64, device=dev)
+        self.ws_barrier = torch.zeros(4, dtype=torch.int32, device=dev)
+        self.stats = torch.zeros(16, dtype=torch.uint8, device=dev)
+
+    @property
+    def x(self):
+        return self._x
+
+    @property
+    def diagonal(self):
+        """Diagonal of the assembled system (equation.py:80-83)."""
+        return self.diag
+
+    def system_struct(self) -> _lib.System_t:
+        return _lib.System_t(self.diag.data_ptr(), self.off.data_ptr(), self.rhs.data_ptr(), self.num_outputs, 0)
+
+    def workspace_struct(self) -> _lib.KrylovWS_t:
+        return _lib.KrylovWS_t(self.ws_vec.data_ptr(), self.ws_partials.data_ptr(), self.ws_results.data_ptr(),
+                               self.ws_barrier.data_ptr())
+
+    def apply(self, x: torch.Tensor) -> torch.Tensor:
+        """y = A x (warp.sparse.bsr_mv)."""
+        x = x.contiguous()
+        y = torch.empty_like(x)
+        m = self.fvm.mesh_struct()
+        _lib.call("wcfd_spmv", ct.byref(m), self.system_struct(), ct.c_void_p(x.data_ptr()),
+                  ct.c_void_p(y.data_ptr()), ct.c_void_p(torch.cuda.current_stream().cuda_stream))
+        return y
+
+    @property
+    def matrix(self):
+        """The system as a torch sparse CSR tensor (C*n x C*n), built on demand."""
+        g = self.fvm._geo
+        C, W, n = g["n_cells"], g["ell_width"], self.num_outputs
+        col = g["ell_col"].long()                       # (W, C)
+        off = self.off[: W * C].reshape(W, C)
+        own = torch.arange(C, device=col.device).expand(W, C)
+        valid = col != own
+        rows, cols, vals = [], [], []
+        for o in range(n):
+            rows.append(n * torch.arange(C, device=col.device) + o)
+            cols.append(n * torch.arange(C, device=col.device) + o)
+            vals.append(self.diag.reshape(C, n)[:, o])
+            rows.append((n * own + o)[valid])
+            cols.append((n * col + o)[valid])
+            vals.append(off[valid])
+        r = torch.cat(rows)
+        c = torch.cat(cols)
+        v = torch.cat(vals)
+        coo = torch.sparse_coo_tensor(torch.stack([r, c]), v, (C * n, C * n)).coalesce()
+        return coo.to_sparse_csr()
+
+    @property
+    def dense(self):
+        return self.matrix.to_dense()
+
+    def add_RHS(self, arr, scale=1.0):
+        self.rhs += arr.reshape(-1) * float(scale)
+
+    def reset(self):
+        self.rhs.zero_()
+        self.diag.zero_()
+        self.off.zero_()
+
+    def solve_Axb(self, x=None):
+        """Krylov solve from x (warm start, in place).  Returns (stats dict, x)."""
+        if x is None:
+            x = self.x
+        m = self.fvm.mesh_struct()
+        fn = "wcfd_bicgstab" if self.linear_solver == "bicgstab" else "wcfd_cg"
+        _lib.call(fn, ct.byref(m), self.system_struct(), ct.c_void_p(x.data_ptr()), self.workspace_struct(),
+                  float(self.tol), int(self.max_iter), ct.c_void_p(self.stats.data_ptr()),
+                  ct.c_void_p(torch.cuda.current_stream().cuda_stream))
+        raw = np.frombuffer(self.stats.cpu().numpy().tobytes(),
+                            dtype=np.dtype([("iterations", "<i4"), ("status", "<i4"), ("residual", "<f8")]))[0]
+        return dict(iterations=int(raw["iterations"]), status=_lib.STATUS_NAMES.get(int(raw["status"]), "?"),
+                    residual=float(raw["residual"])), x

@@ -1,0 +1,181 @@
+// Cell-parallel assembly of the momentum and pressure systems into the fixed
+// per-mesh pattern (diagonal + W slot-major off-diagonals).  Each cell walks its F local
+// faces in slot order and writes only its own row, so no atomics are needed (the
+// reference adds per-face weights with atomics, equation_kernels.py:52-122).
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace wcfd {
+
+// Momentum row of cell c (the reference's rows 3c+o of the interleaved BSR matrix):
+//
+//   convection, upwind (convection.py:43-91, convectionScheme.py:28-52), scale +1
+//     internal face, this cell's side with outward flux F (= +mdot owner, -mdot neighbour):
+//       owner:     w_P = mdot if mdot > 0 else 0 ;  w_N = 0 if mdot > 0 else mdot
+//       neighbour: w_P = 0 if mdot > 0 else -mdot; w_N = -mdot if mdot > 0 else 0
+//     boundary face: rhs -= mdot_b phi_b                                   (Q7)
+//   diffusion, scale -1 (diffusion.py:113-198): internal  w_P = -nu A/d, w_N = +nu A/d
+//     boundary fixed value:     diag += nu A/|r_Pf| ; rhs += nu A/|r_Pf| phi_b
+//     boundary fixed gradient:  rhs += nu g A
+//   ddt (PISO, ddt.py:24-32): diag += V/dt ; rhs += phi_old V/dt
+//   explicit -(1/rho) grad p V (grad.py:20-29, incompressible.py:107)
+//   implicit relaxation (equation_kernels.py:128-152):
+//     rhs += (1-a)/a diag phi ; diag /= a
+//   rUA = V / (diag_u rho) (solver_kernels.py:6-16)
+// Internal-face explicit weights never reach the RHS (equation_kernels.py:84-101), so
+// none are formed here.
+__global__ void __launch_bounds__(kBlock) momentum_assemble_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s,
+                                                                   wcfd_system sys, float* __restrict__ rua,
+                                                                   wcfd_params prm) {
+    const int c = blockIdx.x * kBlock + threadIdx.x;
+    if (c >= m.n_cells) return;
+    const int C = m.n_cells;
+    const float nu = prm.nu;
+    float dsum = 0.0f;
+    float dx[3] = {0.0f, 0.0f, 0.0f};
+    float b[3] = {0.0f, 0.0f, 0.0f};
+    int j = 0;
+    const float4* slots = reinterpret_cast<const float4*>(m.cell_slot);
+    for (int f = 0; f < m.faces_per_cell; ++f) {
+        const int sk = __float_as_int(__ldg(&slots[(size_t)f * C + c].w));
+        const bool owner_side = sk >= 0;
+        const int k = owner_side ? sk : ~sk;
+        const float md = s.mass_fluxes[k];
+        const int N = __ldg(m.face_nbr + k);
+        if (N >= 0) {
+            const float dcoef = nu * __ldg(m.face_gdiff + k);
+            float w0, w1;
+            if (owner_side) {
+                w0 = md > 0.0f ? md : 0.0f;
+                w1 = md > 0.0f ? 0.0f : md;
+            } else {
+                const float mn = -md;
+                w0 = md > 0.0f ? 0.0f : mn;
+                w1 = md > 0.0f ? mn : 0.0f;
+            }
+            dsum += w0 + dcoef;
+            sys.off[(size_t)j * C + c] = w1 - dcoef;
+            ++j;
+        } else {
+            const int br = __ldg(m.face_brow + k);
+            const uchar4 t = __ldg(reinterpret_cast<const uchar4*>(bc.type) + br);
+            const float4 fvb = ld4(s.face_values + 4 * (size_t)k);
+            const float4 fgb = ld4(s.face_gradients + 4 * (size_t)k);
+            const float area = __ldg(m.face_normal + 4 * (size_t)k + 3);
+            const float wd = nu * __ldg(m.face_gdiff + k);
+            const uint8_t tt[3] = {t.x, t.y, t.z};
+#pragma unroll
+            for (int o = 0; o < 3; ++o) {
+                b[o] -= md * comp(fvb, o);
+                if (tt[o] == 2) {
+                    b[o] += nu * comp(fgb, o) * area;
+                } else {
+                    dx[o] += wd;
+                    b[o] += wd * comp(fvb, o);
+                }
+            }
+        }
+    }
+    for (; j < m.ell_width; ++j) sys.off[(size_t)j * C + c] = 0.0f;
+    const float V = __ldg(m.cell_volume + c);
+    const float4 cv = ld4(s.cell_values + 4 * (size_t)c);
+    const float* gp = s.cell_gradients + 12 * (size_t)c + 9;
+    const float neg_inv_rho = -(1.0f / prm.rho);
+    float d[3];
+#pragma unroll
+    for (int o = 0; o < 3; ++o) {
+        d[o] = dsum + dx[o];
+        if (!prm.steady) {
+            const float vd = V / prm.dt;
+            d[o] += vd;
+            b[o] += comp(cv, o) * vd;
+        }
+        b[o] += (gp[o] * V) * neg_inv_rho;
+        if (prm.steady && prm.u_relax > 0.0f) {
+            const float a = prm.u_relax;
+            b[o] += (1.0f - a) / a * d[o] * comp(cv, o);
+            d[o] = d[o] / a;
+        }
+        sys.diag[3 * (size_t)c + o] = d[o];
+        sys.rhs[3 * (size_t)c + o] = b[o];
+    }
+    rua[c] = V / (d[0] * prm.rho);
+}
+
+// Pressure row of cell c: DiffusionTerm('p', nu = rUA_f), scale +1 (diffusion.py:113-198)
+//   internal:          diag -= rUA_f A/d ; off = +rUA_f A/d
+//   boundary value:    diag -= rUA_f A/|r_Pf| ; rhs -= rUA_f A/|r_Pf| p_b
+//   boundary gradient: rhs -= rUA_f g A
+// then rhs += div(HbyA) (incompressible.py:137) and, for the reference cell, the row
+// becomes identity with rhs = value (equation_kernels.py:155-175; its column stays).
+__global__ void __launch_bounds__(kBlock) pressure_assemble_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s,
+                                                                   wcfd_system sys,
+                                                                   const float* __restrict__ rua_faces,
+                                                                   const float* __restrict__ div, wcfd_params prm) {
+    const int c = blockIdx.x * kBlock + threadIdx.x;
+    if (c >= m.n_cells) return;
+    const int C = m.n_cells;
+    float d = 0.0f, b = 0.0f;
+    int j = 0;
+    const bool ref = (c == prm.ref_cell);
+    const float4* slots = reinterpret_cast<const float4*>(m.cell_slot);
+    for (int f = 0; f < m.faces_per_cell; ++f) {
+        const int sk = __float_as_int(__ldg(&slots[(size_t)f * C + c].w));
+        const int k = sk >= 0 ? sk : ~sk;
+        const int N = __ldg(m.face_nbr + k);
+        const float coef = rua_faces[k] * __ldg(m.face_gdiff + k);
+        if (N >= 0) {
+            d -= coef;
+            sys.off[(size_t)j * C + c] = ref ? 0.0f : coef;
+            ++j;
+        } else {
+            const int br = __ldg(m.face_brow + k);
+            const uint8_t t = __ldg(bc.type + 4 * (size_t)br + 3);
+            if (t == 2) {
+                const float area = __ldg(m.face_normal + 4 * (size_t)k + 3);
+                b -= rua_faces[k] * s.face_gradients[4 * (size_t)k + 3] * area;
+            } else {
+                d -= coef;
+                b -= coef * s.face_values[4 * (size_t)k + 3];
+            }
+        }
+    }
+    for (; j < m.ell_width; ++j) sys.off[(size_t)j * C + c] = 0.0f;
+    b += div[c];
+    if (ref) {
+        d = 1.0f;
+        b = prm.ref_value;
+    }
+    sys.diag[c] = d;
+    sys.rhs[c] = b;
+}
+
+// y = A x on the mesh pattern; NC = 1 (scalar) or 3 (momentum: shared off-diagonals,
+// interleaved components).
+template <int NC>
+__global__ void __launch_bounds__(kBlock) spmv_kernel(wcfd_mesh m, wcfd_system A, const float* __restrict__ x,
+                                                      float* __restrict__ y) {
+    const int c = blockIdx.x * kBlock + threadIdx.x;
+    if (c >= m.n_cells) return;
+    const int C = m.n_cells;
+    float acc[NC];
+#pragma unroll
+    for (int o = 0; o < NC; ++o) acc[o] = A.diag[NC * (size_t)c + o] * x[NC * (size_t)c + o];
+    for (int j = 0; j < m.ell_width; ++j) {
+        const float a = A.off[(size_t)j * C + c];
+        const int col = __ldg(m.ell_col + (size_t)j * C + c);
+#pragma unroll
+        for (int o = 0; o < NC; ++o) acc[o] += a * x[NC * (size_t)col + o];
+    }
+#pragma unroll
+    for (int o = 0; o < NC; ++o) y[NC * (size_t)c + o] = acc[o];
+}
+
+void launch_spmv(const wcfd_mesh& m, wcfd_system A, const float* x, float* y, cudaStream_t st) {
+    if (A.ncomp == 1)
+        spmv_kernel<1><<<grid_for(m.n_cells), kBlock, 0, st>>>(m, A, x, y);
+    else
+        spmv_kernel<3><<<grid_for(m.n_cells), kBlock, 0, st>>>(m, A, x, y);
+}
+
+}  // namespace wcfd

@@ -1,0 +1,285 @@
+// extern "C" entry points of libwcfd.so (declared in include/wcfd.h).
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+using namespace wcfd;
+
+namespace {
+
+thread_local char g_last_error[512] = "";
+
+int set_error(int code, const char* what) {
+    std::snprintf(g_last_error, sizeof(g_last_error), "%s", what);
+    return code;
+}
+
+int check_launch(const char* what) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s", what, cudaGetErrorString(e));
+        return WCFD_ERR_CUDA;
+    }
+    return WCFD_OK;
+}
+
+#define RET_IF(cond, code, msg) \
+    do {                        \
+        if (cond) return set_error(code, msg); \
+    } while (0)
+#define LAUNCH_CHECK(what)                 \
+    do {                                   \
+        const int rc_ = check_launch(what); \
+        if (rc_ != WCFD_OK) return rc_;     \
+    } while (0)
+
+int check_mesh(const wcfd_mesh* m) {
+    if (!m) return set_error(WCFD_ERR_ARGUMENT, "mesh is null");
+    if (m->n_cells <= 0 || m->n_faces <= 0) return set_error(WCFD_ERR_ARGUMENT, "empty mesh");
+    if (m->faces_per_cell < 1 || m->faces_per_cell > kMaxSlots)
+        return set_error(WCFD_ERR_ARGUMENT, "faces_per_cell must be in 1..6");
+    if (m->ell_width < 0 || m->ell_width > m->faces_per_cell)
+        return set_error(WCFD_ERR_ARGUMENT, "ell_width must be in 0..faces_per_cell");
+    if (!m->face_owner || !m->face_nbr || !m->face_brow || !m->face_interp || !m->face_normal ||
+        !m->face_gdiff || !m->face_rpf || !m->cell_slot || !m->cell_volume || !m->ell_col)
+        return set_error(WCFD_ERR_ARGUMENT, "mesh has a null array");
+    return WCFD_OK;
+}
+
+inline cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// co-resident blocks of a cooperative kernel on the current device (cached per device)
+int coop_capacity(const void* fn, int slot) {
+    static std::mutex mu;
+    static int cache[2][64];
+    static bool init = false;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(mu);
+    if (!init) {
+        std::memset(cache, 0, sizeof(cache));
+        init = true;
+    }
+    if (dev < 64 && cache[slot][dev] > 0) return cache[slot][dev];
+    int per_sm = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kSolverBlock, 0);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int cap = per_sm * sms;
+    if (cap > WCFD_MAX_BLOCKS) cap = WCFD_MAX_BLOCKS;
+    if (dev < 64) cache[slot][dev] = cap;
+    return cap;
+}
+
+int launch_krylov(const void* fn, int slot, const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws,
+                  double atol, int maxiter, wcfd_solve_stats* stats, cudaStream_t st, const char* name) {
+    int rc = check_mesh(m);
+    if (rc) return rc;
+    RET_IF(!A.diag || !A.off || !A.rhs || !x || !ws.vec || !ws.partials || !ws.results || !ws.barrier || !stats,
+           WCFD_ERR_ARGUMENT, "null solver argument");
+    RET_IF(maxiter < 0 || !(atol >= 0.0), WCFD_ERR_ARGUMENT, "bad atol or maxiter");
+    const int cap = coop_capacity(fn, slot);
+    LAUNCH_CHECK("occupancy query");
+    RET_IF(cap <= 0, WCFD_ERR_CUDA, "solver kernel cannot be resident");
+    long long want = (m->n_cells + kSolverBlock - 1) / kSolverBlock;
+    int grid = (int)(want < cap ? want : cap);
+    if (grid < 1) grid = 1;
+    if (cudaMemsetAsync(ws.barrier, 0, 4 * sizeof(uint32_t), st) != cudaSuccess)
+        return set_error(WCFD_ERR_CUDA, "barrier reset failed");
+    KrylovArgs a;
+    a.m = *m;
+    a.A = A;
+    a.x = x;
+    a.ws = ws.vec;
+    a.g.partials = ws.partials;
+    a.g.results = ws.results;
+    a.g.bar = ws.barrier;
+    a.g.err = reinterpret_cast<int*>(ws.barrier + 2);
+    a.atol2 = atol * atol;
+    a.maxiter = maxiter;
+    a.stats = stats;
+    void* args[] = {&a};
+    const cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kSolverBlock), args, 0, st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s", name, cudaGetErrorString(e));
+        return WCFD_ERR_CUDA;
+    }
+    return WCFD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wcfd_version(void) { return 100; }
+
+const char* wcfd_last_error(void) { return g_last_error; }
+
+int64_t wcfd_krylov_workspace_floats(int32_t n_cells, int32_t ncomp) {
+    if (n_cells <= 0 || (ncomp != 1 && ncomp != 3)) return -1;
+    return ncomp == 1 ? 4LL * n_cells : 18LL * n_cells;
+}
+
+int wcfd_face_pass_flags(const wcfd_mesh* m, wcfd_bc bc, wcfd_state s, uint32_t mask, uint32_t flags,
+                         void* stream) {
+    int rc = check_mesh(m);
+    if (rc) return rc;
+    RET_IF(mask > WCFD_ALL || flags > 15u, WCFD_ERR_ARGUMENT, "bad mask or flags");
+    RET_IF(!bc.type || !bc.value || !s.cell_values || !s.cell_gradients || !s.face_values || !s.face_gradients ||
+               !s.mass_fluxes,
+           WCFD_ERR_ARGUMENT, "null field");
+    face_pass_kernel<<<grid_for(m->n_faces), kBlock, 0, S(stream)>>>(*m, bc, s, mask, flags);
+    LAUNCH_CHECK("face_pass_kernel");
+    return WCFD_OK;
+}
+
+int wcfd_set_boundary_conditions(const wcfd_mesh* m, wcfd_bc bc, wcfd_state s, void* stream) {
+    return wcfd_face_pass_flags(m, bc, s, 0u, 1u, stream);
+}
+
+int wcfd_face_interpolation(const wcfd_mesh* m, wcfd_bc bc, wcfd_state s, uint32_t mask, int32_t skew,
+                            int32_t upwind, void* stream) {
+    return wcfd_face_pass_flags(m, bc, s, mask, (skew ? 4u : 0u) | (upwind ? 8u : 0u), stream);
+}
+
+int wcfd_calculate_mass_flux(const wcfd_mesh* m, wcfd_state s, void* stream) {
+    int rc = check_mesh(m);
+    if (rc) return rc;
+    RET_IF(!s.face_values || !s.mass_fluxes, WCFD_ERR_ARGUMENT, "null field");
+    mass_flux_kernel<<<grid_for(m->n_faces), kBlock, 0, S(stream)>>>(*m, s);
+    LAUNCH_CHECK("mass_flux_kernel");
+    return WCFD_OK;
+}
+
+int wcfd_calculate_gradients(const wcfd_mesh* m, wcfd_state s, uint32_t mask, void* stream) {
+    int rc = check_mesh(m);
+    if (rc) return rc;
+    RET_IF(mask > WCFD_ALL, WCFD_ERR_ARGUMENT, "bad mask");
+    RET_IF(!s.cell_gradients || !s.face_values, WCFD_ERR_ARGUMENT, "null field");
+    gradient_kernel<<<grid_for(m->n_cells), kBlock, 0, S(stream)>>>(*m, s, mask, nullptr, CorrectArgs{nullptr, nullptr});
+    LAUNCH_CHECK("gradient_kernel");
+    return WCFD_OK;
+}
+
+int wcfd_div_flux(const wcfd_mesh* m, const float* mass_fluxes, float* div, void* stream) {
+    int rc = check_mesh(m);
+    if (rc) return rc;
+    RET_IF(!mass_fluxes || !div, WCFD_ERR_ARGUMENT, "null array");
+    div_kernel<<<grid_for(m->n_cells), kBlock, 0, S(stream)>>>(*m, mass_fluxes, div);
+    LAUNCH_CHECK("div_kernel");
+    return WCFD_OK;
+}
+
+int wcfd_cell_to_face(const wcfd_mesh* m, const float* cell, float* face, void* stream) {
+    int rc = check_mesh(m);
+    if (rc) return rc;
+    RET_IF(!cell || !face, WCFD_ERR_ARGUMENT, "null array");
+    cell_to_face_kernel<<<grid_for(m->n_faces), kBlock, 0, S(stream)>>>(*m, cell, face);
+    LAUNCH_CHECK("cell_to_face_kernel");
+    return WCFD_OK;
+}
+
+int wcfd_assemble_momentum(const wcfd_case* c, void* stream) {
+    RET_IF(!c, WCFD_ERR_ARGUMENT, "case is null");
+    int rc = check_mesh(&c->mesh);
+    if (rc) return rc;
+    RET_IF(!c->mom.diag || !c->mom.off || !c->mom.rhs || !c->rua, WCFD_ERR_ARGUMENT, "null momentum array");
+    RET_IF(c->prm.rho == 0.0f || (!c->prm.steady && c->prm.dt <= 0.0f), WCFD_ERR_ARGUMENT, "bad rho or dt");
+    momentum_assemble_kernel<<<grid_for(c->mesh.n_cells), kBlock, 0, S(stream)>>>(c->mesh, c->bc, c->state, c->mom,
+                                                                                 c->rua, c->prm);
+    LAUNCH_CHECK("momentum_assemble_kernel");
+    return WCFD_OK;
+}
+
+int wcfd_assemble_pressure(const wcfd_case* c, void* stream) {
+    RET_IF(!c, WCFD_ERR_ARGUMENT, "case is null");
+    int rc = check_mesh(&c->mesh);
+    if (rc) return rc;
+    RET_IF(!c->pres.diag || !c->pres.off || !c->pres.rhs || !c->rua_faces || !c->div, WCFD_ERR_ARGUMENT,
+           "null pressure array");
+    RET_IF(c->prm.ref_cell >= c->mesh.n_cells, WCFD_ERR_ARGUMENT, "reference cell out of range");
+    pressure_assemble_kernel<<<grid_for(c->mesh.n_cells), kBlock, 0, S(stream)>>>(c->mesh, c->bc, c->state, c->pres,
+                                                                                 c->rua_faces, c->div, c->prm);
+    LAUNCH_CHECK("pressure_assemble_kernel");
+    return WCFD_OK;
+}
+
+int wcfd_spmv(const wcfd_mesh* m, wcfd_system A, const float* x, float* y, void* stream) {
+    int rc = check_mesh(m);
+    if (rc) return rc;
+    RET_IF(!A.diag || !A.off || !x || !y, WCFD_ERR_ARGUMENT, "null array");
+    RET_IF(A.ncomp != 1 && A.ncomp != 3, WCFD_ERR_ARGUMENT, "ncomp must be 1 or 3");
+    launch_spmv(*m, A, x, y, S(stream));
+    LAUNCH_CHECK("spmv_kernel");
+    return WCFD_OK;
+}
+
+int wcfd_cg(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, double atol, int32_t maxiter,
+            wcfd_solve_stats* stats, void* stream) {
+    RET_IF(A.ncomp != 1, WCFD_ERR_ARGUMENT, "cg solves scalar systems (ncomp 1)");
+    return launch_krylov((const void*)cg_kernel, 0, m, A, x, ws, atol, maxiter, stats, S(stream), "cg_kernel");
+}
+
+int wcfd_bicgstab(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, double atol, int32_t maxiter,
+                  wcfd_solve_stats* stats, void* stream) {
+    RET_IF(A.ncomp != 3, WCFD_ERR_ARGUMENT, "bicgstab solves the 3-component momentum system (ncomp 3)");
+    return launch_krylov((const void*)bicgstab_kernel, 1, m, A, x, ws, atol, maxiter, stats, S(stream),
+                         "bicgstab_kernel");
+}
+
+int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
+    RET_IF(!cp, WCFD_ERR_ARGUMENT, "case is null");
+    const wcfd_case& c = *cp;
+    int rc = check_mesh(&c.mesh);
+    if (rc) return rc;
+    RET_IF(!c.hbya || !c.p_x || !c.rua || !c.rua_faces || !c.div || !c.stats, WCFD_ERR_ARGUMENT, "null case array");
+    RET_IF(c.prm.n_inner < 0 || c.prm.n_ortho < 0, WCFD_ERR_ARGUMENT, "negative loop count");
+    cudaStream_t st = S(stream);
+    const wcfd_mesh& m = c.mesh;
+    const uint32_t skew = c.prm.skew ? 4u : 0u;
+    const int gf = grid_for(m.n_faces), gc = grid_for(m.n_cells);
+    // incompressible.py:96-99
+    face_pass_kernel<<<gf, kBlock, 0, st>>>(m, c.bc, c.state, WCFD_ALL, 1u | 2u | skew);
+    LAUNCH_CHECK("face_pass_kernel");
+    gradient_kernel<<<gc, kBlock, 0, st>>>(m, c.state, WCFD_ALL, nullptr, CorrectArgs{nullptr, nullptr});
+    LAUNCH_CHECK("gradient_kernel");
+    // :102-116
+    rc = wcfd_assemble_momentum(cp, stream);
+    if (rc) return rc;
+    rc = wcfd_bicgstab(&m, c.mom, c.hbya, c.ws_u, c.prm.atol_u, c.prm.maxiter, c.stats + 0, stream);
+    if (rc) return rc;
+    // :118-123
+    hbya_kernel<<<gc, kBlock, 0, st>>>(m.n_cells, c.state.cell_gradients, c.rua, c.hbya, c.state.cell_values);
+    LAUNCH_CHECK("hbya_kernel");
+    cell_to_face_kernel<<<gf, kBlock, 0, st>>>(m, c.rua, c.rua_faces);
+    LAUNCH_CHECK("cell_to_face_kernel");
+    for (int inner = 0; inner < c.prm.n_inner; ++inner) {
+        for (int ortho = 0; ortho < c.prm.n_ortho; ++ortho) {
+            // :127-132
+            face_pass_kernel<<<gf, kBlock, 0, st>>>(m, c.bc, c.state, WCFD_ALL, 2u | skew);
+            LAUNCH_CHECK("face_pass_kernel");
+            gradient_kernel<<<gc, kBlock, 0, st>>>(m, c.state, WCFD_ALL, c.div, CorrectArgs{nullptr, nullptr});
+            LAUNCH_CHECK("gradient_kernel");
+            // :134-142
+            rc = wcfd_assemble_pressure(cp, stream);
+            if (rc) return rc;
+            rc = wcfd_cg(&m, c.pres, c.p_x, c.ws_p, c.prm.atol_p, c.prm.maxiter, c.stats + 1, stream);
+            if (rc) return rc;
+            // :144-147
+            p_update_kernel<<<gc, kBlock, 0, st>>>(m.n_cells, c.p_x, c.state.cell_values,
+                                                   c.prm.steady ? c.prm.p_relax : 0.0f);
+            LAUNCH_CHECK("p_update_kernel");
+            // :150-156
+            face_pass_kernel<<<gf, kBlock, 0, st>>>(m, c.bc, c.state, WCFD_P, skew);
+            LAUNCH_CHECK("face_pass_kernel");
+            gradient_kernel<<<gc, kBlock, 0, st>>>(m, c.state, WCFD_P, nullptr, CorrectArgs{c.hbya, c.rua});
+            LAUNCH_CHECK("gradient_kernel");
+        }
+    }
+    return WCFD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,196 @@
+// Field operators of the finite-volume step: boundary values + face interpolation
+// (+ mass flux), Green-Gauss gradients (+ divergence of the mass flux), cell -> face
+// interpolation.  One thread per face or per cell; no atomics, so every result is
+// bit-reproducible.
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace wcfd {
+
+// Face pass (warp_cfd: conditions.py:5-19, interpolation_kernels.py:5-54,
+// interpolation_functions.py:5-28, skewness_functions.py:6-19, model_kernels.py:45-60).
+//   internal face: phi_f = psi phi_P + (1-psi) phi_N
+//                          + (psi grad_P + (1-psi) grad_N) . (r_f - (psi r_P + (1-psi) r_N))
+//   boundary face: fixed value -> phi_f = value; fixed gradient g -> phi_f = phi_P + |r_Pf| g
+//   mass flux:     mdot = (u_f, v_f, w_f) . n_owner * A
+// flags: bit0 apply every field's boundary table first (set_boundary_conditions),
+//        bit1 recompute the mass flux, bit2 skew correction, bit3 upwind instead of
+//        linear interpolation on internal faces (phi_P if mdot > 0 else phi_N,
+//        interpolation_functions.py:18-28; used by face_interpolation(upwind=True)).
+__global__ void __launch_bounds__(kBlock) face_pass_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s,
+                                                           uint32_t mask, uint32_t flags) {
+    const int k = blockIdx.x * kBlock + threadIdx.x;
+    if (k >= m.n_faces) return;
+    const int P = __ldg(m.face_owner + k);
+    const int N = __ldg(m.face_nbr + k);
+    float4 fv = ld4(s.face_values + 4 * (size_t)k);
+    const float4 cp = ld4(s.cell_values + 4 * (size_t)P);
+    if (N >= 0) {
+        const float4 gi = __ldg(reinterpret_cast<const float4*>(m.face_interp) + k);
+        const float psi = gi.w;
+        const float psi2 = 1.0f - psi;
+        const float4 cn = ld4(s.cell_values + 4 * (size_t)N);
+        const float* gP = s.cell_gradients + 12 * (size_t)P;
+        const float* gN = s.cell_gradients + 12 * (size_t)N;
+#pragma unroll
+        for (int o = 0; o < 4; ++o) {
+            if (!(mask & (1u << o))) continue;
+            float val;
+            if (flags & 8u) val = s.mass_fluxes[k] > 0.0f ? comp(cp, o) : comp(cn, o);
+            else val = comp(cp, o) * psi + psi2 * comp(cn, o);
+            if (flags & 4u) {
+                const float gx = gP[3 * o + 0] * psi + psi2 * gN[3 * o + 0];
+                const float gy = gP[3 * o + 1] * psi + psi2 * gN[3 * o + 1];
+                const float gz = gP[3 * o + 2] * psi + psi2 * gN[3 * o + 2];
+                val += gx * gi.x + gy * gi.y + gz * gi.z;
+            }
+            set_comp(fv, o, val);
+        }
+    } else {
+        const int b = __ldg(m.face_brow + k);
+        const uchar4 t = __ldg(reinterpret_cast<const uchar4*>(bc.type) + b);
+        const float4 bv = __ldg(reinterpret_cast<const float4*>(bc.value) + b);
+        float4 fg = ld4(s.face_gradients + 4 * (size_t)k);
+        const uint8_t tt[4] = {t.x, t.y, t.z, t.w};
+        if (flags & 1u) {
+#pragma unroll
+            for (int o = 0; o < 4; ++o) {
+                if (tt[o] == 1) set_comp(fv, o, comp(bv, o));
+                else if (tt[o] == 2) set_comp(fg, o, comp(bv, o));
+            }
+            st4(s.face_gradients + 4 * (size_t)k, fg);
+        }
+        const float rpf = __ldg(m.face_rpf + k);
+#pragma unroll
+        for (int o = 0; o < 4; ++o) {
+            if ((mask & (1u << o)) && tt[o] == 2) set_comp(fv, o, rpf * comp(fg, o) + comp(cp, o));
+        }
+    }
+    st4(s.face_values + 4 * (size_t)k, fv);
+    if (flags & 2u) {
+        const float4 n = __ldg(reinterpret_cast<const float4*>(m.face_normal) + k);
+        s.mass_fluxes[k] = (fv.x * n.x + fv.y * n.y + fv.z * n.z) * n.w;
+    }
+}
+
+// Green-Gauss gradient (model.py:232-239, model_kernels.py:71-90):
+//   grad phi_c = sum_f phi_f A_f n_cf / V_c, gathered per cell in slot order.
+// Fields outside `mask` get a zero gradient (the reference zeroes the whole array).
+// With `div` != null also div[c] = sum_f (+-) mdot_f (model_kernels.py:26-34).
+// With `corr` != null (the pressure correction of incompressible.py:150-156) also
+//   HbyA[c] -= rUA[c] grad p ; cell u,v,w = HbyA.
+__global__ void __launch_bounds__(kBlock) gradient_kernel(wcfd_mesh m, wcfd_state s, uint32_t mask,
+                                                          float* __restrict__ div, CorrectArgs corr) {
+    const int c = blockIdx.x * kBlock + threadIdx.x;
+    if (c >= m.n_cells) return;
+    const int C = m.n_cells;
+    float g[4][3];
+#pragma unroll
+    for (int o = 0; o < 4; ++o) g[o][0] = g[o][1] = g[o][2] = 0.0f;
+    float dv = 0.0f;
+    const float4* slots = reinterpret_cast<const float4*>(m.cell_slot);
+    for (int f = 0; f < m.faces_per_cell; ++f) {
+        const float4 sl = __ldg(slots + (size_t)f * C + c);
+        const int sk = __float_as_int(sl.w);
+        const int k = sk >= 0 ? sk : ~sk;
+        const float4 fv = ld4(s.face_values + 4 * (size_t)k);
+#pragma unroll
+        for (int o = 0; o < 4; ++o) {
+            if (!(mask & (1u << o))) continue;
+            const float phi = comp(fv, o);
+            g[o][0] += phi * sl.x;
+            g[o][1] += phi * sl.y;
+            g[o][2] += phi * sl.z;
+        }
+        if (div) {
+            const float md = s.mass_fluxes[k];
+            dv += sk >= 0 ? md : -md;
+        }
+    }
+    float* gc = s.cell_gradients + 12 * (size_t)c;
+    st4(gc + 0, make_float4(g[0][0], g[0][1], g[0][2], g[1][0]));
+    st4(gc + 4, make_float4(g[1][1], g[1][2], g[2][0], g[2][1]));
+    st4(gc + 8, make_float4(g[2][2], g[3][0], g[3][1], g[3][2]));
+    if (div) div[c] = dv;
+    if (corr.hbya) {
+        const float r = corr.rua[c];
+        float* h = corr.hbya + 3 * (size_t)c;
+        const float hx = h[0] - g[3][0] * r;
+        const float hy = h[1] - g[3][1] * r;
+        const float hz = h[2] - g[3][2] * r;
+        h[0] = hx; h[1] = hy; h[2] = hz;
+        float* cv = s.cell_values + 4 * (size_t)c;
+        cv[0] = hx; cv[1] = hy; cv[2] = hz;
+    }
+}
+
+// mdot = (u_f, v_f, w_f) . n_owner * A (model_kernels.py:45-60)
+__global__ void __launch_bounds__(kBlock) mass_flux_kernel(wcfd_mesh m, wcfd_state s) {
+    const int k = blockIdx.x * kBlock + threadIdx.x;
+    if (k >= m.n_faces) return;
+    const float4 fv = ld4(s.face_values + 4 * (size_t)k);
+    const float4 n = __ldg(reinterpret_cast<const float4*>(m.face_normal) + k);
+    s.mass_fluxes[k] = (fv.x * n.x + fv.y * n.y + fv.z * n.z) * n.w;
+}
+
+// div[c] = sum over the cell's faces of +mdot (owner side) or -mdot (model_kernels.py:26-34)
+__global__ void __launch_bounds__(kBlock) div_kernel(wcfd_mesh m, const float* __restrict__ mdot,
+                                                     float* __restrict__ div) {
+    const int c = blockIdx.x * kBlock + threadIdx.x;
+    if (c >= m.n_cells) return;
+    const int C = m.n_cells;
+    const float4* slots = reinterpret_cast<const float4*>(m.cell_slot);
+    float dv = 0.0f;
+    for (int f = 0; f < m.faces_per_cell; ++f) {
+        const int sk = __float_as_int(__ldg(&slots[(size_t)f * C + c].w));
+        const float md = mdot[sk >= 0 ? sk : ~sk];
+        dv += sk >= 0 ? md : -md;
+    }
+    div[c] = dv;
+}
+
+// interpolate_cell_value_to_face (solver_kernels.py:21-36)
+__global__ void __launch_bounds__(kBlock) cell_to_face_kernel(wcfd_mesh m, const float* __restrict__ x,
+                                                              float* __restrict__ y) {
+    const int k = blockIdx.x * kBlock + threadIdx.x;
+    if (k >= m.n_faces) return;
+    const int P = __ldg(m.face_owner + k);
+    const int N = __ldg(m.face_nbr + k);
+    if (N < 0) {
+        y[k] = x[P];
+    } else {
+        const float psi = __ldg(m.face_interp + 4 * (size_t)k + 3);
+        y[k] = psi * x[P] + (1.0f - psi) * x[N];
+    }
+}
+
+// After the momentum solve (incompressible.py:118-123):
+//   HbyA += rUA grad p ; cell u,v,w = HbyA.
+// Optionally rUA_f as in cell_to_face for the faces of the same index range.
+__global__ void __launch_bounds__(kBlock) hbya_kernel(int C, const float* __restrict__ grad,
+                                                      const float* __restrict__ rua, float* __restrict__ hbya,
+                                                      float* __restrict__ cell_values) {
+    const int c = blockIdx.x * kBlock + threadIdx.x;
+    if (c >= C) return;
+    const float r = rua[c];
+    const float* gp = grad + 12 * (size_t)c + 9;
+    float* h = hbya + 3 * (size_t)c;
+    const float hx = h[0] + gp[0] * r;
+    const float hy = h[1] + gp[1] * r;
+    const float hz = h[2] + gp[2] * r;
+    h[0] = hx; h[1] = hy; h[2] = hz;
+    float* cv = cell_values + 4 * (size_t)c;
+    cv[0] = hx; cv[1] = hy; cv[2] = hz;
+}
+
+// p = alpha p_new + (1 - alpha) p (model.py:381-384), or p = p_new (alpha <= 0).
+__global__ void __launch_bounds__(kBlock) p_update_kernel(int C, const float* __restrict__ p_new,
+                                                          float* __restrict__ cell_values, float alpha) {
+    const int c = blockIdx.x * kBlock + threadIdx.x;
+    if (c >= C) return;
+    float* p = cell_values + 4 * (size_t)c + 3;
+    if (alpha > 0.0f) *p = alpha * p_new[c] + (1.0f - alpha) * *p;
+    else *p = p_new[c];
+}
+
+}  // namespace wcfd

@@ -1,0 +1,45 @@
+// Kernel declarations shared between the .cu files of libwcfd.
+#pragma once
+
+#include "common.cuh"
+
+namespace wcfd {
+
+struct CorrectArgs {
+    float* hbya;        // null = no velocity correction
+    const float* rua;
+};
+
+__global__ void face_pass_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s, uint32_t mask, uint32_t flags);
+__global__ void gradient_kernel(wcfd_mesh m, wcfd_state s, uint32_t mask, float* div, CorrectArgs corr);
+__global__ void mass_flux_kernel(wcfd_mesh m, wcfd_state s);
+__global__ void div_kernel(wcfd_mesh m, const float* mdot, float* div);
+__global__ void cell_to_face_kernel(wcfd_mesh m, const float* x, float* y);
+__global__ void hbya_kernel(int C, const float* grad, const float* rua, float* hbya, float* cell_values);
+__global__ void p_update_kernel(int C, const float* p_new, float* cell_values, float alpha);
+
+__global__ void momentum_assemble_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s, wcfd_system sys,
+                                         float* rua, wcfd_params prm);
+__global__ void pressure_assemble_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s, wcfd_system sys,
+                                         const float* rua_faces, const float* div, wcfd_params prm);
+
+// y = A x (NC = A.ncomp), launched from assemble.cu where the kernel template lives
+void launch_spmv(const wcfd_mesh& m, wcfd_system A, const float* x, float* y, cudaStream_t st);
+
+// persistent Krylov kernels (cooperative launch)
+struct KrylovArgs {
+    wcfd_mesh m;
+    wcfd_system A;
+    float* x;
+    float* ws;            // workspace vectors
+    GridCtl g;
+    double atol2;
+    int maxiter;
+    wcfd_solve_stats* stats;
+};
+__global__ void cg_kernel(KrylovArgs a);
+__global__ void bicgstab_kernel(KrylovArgs a);
+
+inline int grid_for(long long n, int bs = kBlock) { return (int)((n + bs - 1) / bs); }
+
+}  // namespace wcfd
