@@ -1,0 +1,358 @@
+"""Benchmark of the SIMPLE outer iteration (cell-iterations/s) on GB300.
+
+Default workload: steady channel flow, 400 x 80 x 1 hexes on a 10 x 1 domain, uniform
+inlet u = 1, outlet p = 0, no-slip walls, Re = 200, relaxation 0.7 / 0.3, fp32 fields
+with fp64 Krylov reductions.  One step = one SIMPLE outer iteration (momentum BiCGSTAB +
+pressure CG, up to 500 iterations each, atol 1e-5).  Synthetic seeded mesh, zero
+initial fields.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload channel|cavity|cavity3d]
+  python bench.py --impl reference ...   # the CPU restatement of the reference algorithm
+
+Timing: W untimed steps, then K steps, each bracketed by CUDA events on the solver
+stream; between steps a 256 MiB buffer is written to flush L2 (the flush is outside the
+events).  A barrier and torch.cuda.synchronize() bracket the timed region; the time is
+the max over ranks.  Under torchrun every rank runs its own case (replicas: the path
+does not shard), so scaling is weak.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (description, builder args)
+    "channel": "steady channel 400x80x1 hex on 10x1, u_in=1, p_out=0, Re=200, SIMPLE 0.7/0.3, fp32 (fp64 reductions)",
+    "cavity": "lid-driven cavity 64x64x1 hex, lid u=1, Re=100, SIMPLE 0.7/0.3, fp32 (fp64 reductions)",
+    "cavity3d": "3D lid-driven cavity 128^3 hex, lid u=1, Re=400, SIMPLE 0.7/0.3, fp32 (fp64 reductions)",
+}
+METRIC = "cell-iterations/s"
+
+
+def build_mesh(workload):
+    from warpcfd_gb300.preprocess import Mesh, create_2D_grid, create_3D_grid, define_boundary_walls
+
+    if workload == "channel":
+        m = Mesh(create_2D_grid((0, 0, 0), 400, 80, 10.0, 1.0, 0.1))
+    elif workload == "cavity":
+        m = Mesh(create_2D_grid((0, 0, 0), 64, 64, 1.0, 1.0, 0.1))
+    elif workload == "cavity3d":
+        m = Mesh(create_3D_grid((0, 0, 0), 128, 128, 128, 1.0, 1.0, 1.0))
+    else:
+        raise ValueError(workload)
+    define_boundary_walls(m)
+    return m
+
+
+def case_setup(workload):
+    """(nu, rho, reference cell, bc function) of a workload."""
+    if workload == "channel":
+        def bc(b):
+            b.velocity_BC("-X", u=1.0, v=0.0, w=0.0)
+            b.pressure_BC("+X", p=0.0)
+            b.no_slip_wall("-Y")
+            b.no_slip_wall("+Y")
+            b.slip_wall("-Z")
+            b.slip_wall("+Z")
+        return 1.0 / 200.0, 1.0, None, bc
+    if workload == "cavity":
+        def bc(b):
+            b.no_slip_wall("-X")
+            b.no_slip_wall("+X")
+            b.no_slip_wall("-Y")
+            b.velocity_BC("+Y", u=1.0, v=0.0, w=0.0)
+            b.slip_wall("+Z")
+            b.slip_wall("-Z")
+        return 0.01, 1.0, 0, bc
+    if workload == "cavity3d":
+        def bc(b):
+            for w in ("-X", "+X", "-Y", "-Z", "+Z"):
+                b.no_slip_wall(w)
+            b.velocity_BC("+Y", u=1.0, v=0.0, w=0.0)
+        return 1.0 / 400.0, 1.0, 0, bc
+    raise ValueError(workload)
+
+
+def build_gpu_case(workload, mesh):
+    from warpcfd_gb300.FV import FVM
+    from warpcfd_gb300.FV.implicit_Solvers import IncompressibleSolver
+
+    nu, rho, ref, bc = case_setup(workload)
+    model = FVM(mesh)
+    model.material.create_incompressible_newtonian_fluid(viscosity=nu * rho, density=rho)
+    if ref is not None:
+        model.set_reference_pressure(ref, 0.0)
+    bc(model.boundary)
+    model.finalize()
+    solver = IncompressibleSolver(model, 0.7, 0.3)
+    solver.verbose = False
+    return model, solver
+
+
+def build_oracle_case(workload, mesh, T=np.float32):
+    from oracle.simple_ref import OracleCase, geometry_from_mesh
+    from warpcfd_gb300.FV.boundary import Boundary
+    from warpcfd_gb300.FV.field import Field
+
+    nu, rho, ref, bc = case_setup(workload)
+    fields = {k: Field(k, i) for i, k in enumerate("uvwp")}
+    b = Boundary(fields, mesh.groups, mesh.face_properties.boundary_face_ids)
+    bc(b)
+    b.check()
+    return OracleCase(geometry_from_mesh(mesh), b.boundary_type, b.boundary_values, nu * rho, rho, T=T,
+                      reference_cell=ref)
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index, enabled=True):
+        self.index = index
+        self.enabled = enabled
+        self.p = None
+
+    def __enter__(self):
+        if not self.enabled:
+            return self
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "100"], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+                self.out = ""
+
+    def summary(self):
+        rows = []
+        for ln in (self.out or "").strip().splitlines():
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        reasons = set()
+        for r in rows:
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
+                               r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(rows[0][2]) if rows[0][2].replace(".", "").isdigit() else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def cpu_baseline(workload, mesh, seconds=15.0, warm=3):
+    """The oracle (fp32, the same algorithm) on this host: ``warm`` untimed outer
+    iterations from zero fields, then as many timed ones as fit in ~``seconds``."""
+    oc = build_oracle_case(workload, mesh)
+    oc.run(0.7, 0.3, n_outer=warm)
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        oc.run(0.7, 0.3, n_outer=1)
+        n += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": mesh.num_cells * n / dt, "unit": METRIC, "cores": 1, "kind": "port",
+            "sample": f"{n} SIMPLE outer iterations (after {warm} untimed) of the same {workload} case, numpy/scipy "
+                      f"fp32 restatement (oracle/simple_ref.py), single thread"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    mesh = build_mesh(args.workload)
+    oc = build_oracle_case(args.workload, mesh)
+    oc.run(0.7, 0.3, n_outer=args.warmup)
+    # each step is one full outer iteration of the workload; stop early (and say so) if
+    # the K steps would not end within --ref-seconds
+    t0 = time.perf_counter()
+    done = 0
+    while done < args.steps:
+        oc.run(0.7, 0.3, n_outer=1)
+        done += 1
+        if time.perf_counter() - t0 > args.ref_seconds:
+            break
+    dt = time.perf_counter() - t0
+    v = mesh.num_cells * done / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus,
+            "steps": done, "steps_requested": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / done,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOADS[args.workload], "cells": mesh.num_cells},
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": 1, "kind": "port",
+                             "sample": f"{done} SIMPLE outer iterations after {args.warmup} untimed, numpy/"
+                                       "scipy fp32 restatement of the reference algorithm (warp-lang is not "
+                                       "installable here), single thread"},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+
+    from warpcfd_gb300 import perfmodel
+    from warpcfd_gb300.build import build_library
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    build_library()
+    mesh = build_mesh(args.workload)
+    model, solver = build_gpu_case(args.workload, mesh)
+    C = mesh.num_cells
+    g = model._geo_host
+    K, B, F, W = g["n_faces"], g["n_bfaces"], g["faces_per_cell"], g["ell_width"]
+    Ki = K - B
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        solver.step()
+    torch.cuda.synchronize()
+
+    K_ = args.steps
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * K_)]
+    kev = [torch.cuda.Event(enable_timing=True) for _ in range(4 * K_)]
+    for e in kev:
+        e.record(stream)          # materialise the CUDA events before handing them to the C side
+    stats_hist = torch.zeros((K_, solver.stats.numel()), dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local, enabled=not args.no_clocks) as clocks:
+        for i in range(K_):
+            flush.zero_()
+            solver.set_timing_events(kev[4 * i: 4 * i + 4])
+            ev[2 * i].record(stream)
+            solver.step()
+            ev[2 * i + 1].record(stream)
+            stats_hist[i].copy_(solver.stats)
+        torch.cuda.synchronize()
+    solver.set_timing_events(None)
+    if dist is not None:
+        dist.barrier()
+    step_ms = np.array([ev[2 * i].elapsed_time(ev[2 * i + 1]) for i in range(K_)])
+    bicg_ms = np.array([kev[4 * i].elapsed_time(kev[4 * i + 1]) for i in range(K_)])
+    cg_ms = np.array([kev[4 * i + 2].elapsed_time(kev[4 * i + 3]) for i in range(K_)])
+    from warpcfd_gb300.FV.implicit_Solvers.incompressible import STATS_DTYPE
+    hist = np.frombuffer(stats_hist.cpu().numpy().tobytes(), dtype=STATS_DTYPE).reshape(K_, 2)
+    k_u = hist[:, 0]["iterations"].astype(np.int64)
+    k_p = hist[:, 1]["iterations"].astype(np.int64)
+    total_ms = float(step_ms.sum())
+    if dist is not None:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * C * K_ / (total_ms * 1e-3)
+
+    # end to end through the public API with host buffers (H2D inputs, D2H result per step)
+    host_in = torch.empty((C, 4), dtype=torch.float32).pin_memory()
+    host_out = torch.empty((C, 4), dtype=torch.float32).pin_memory()
+    host_in.copy_(model.cell_values.cpu())
+    K_e2e = max(1, K_ // 2)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(K_e2e):
+        model.cell_values.copy_(host_in, non_blocking=True)
+        solver.step()
+        host_out.copy_(model.cell_values, non_blocking=True)
+        torch.cuda.synchronize()
+        host_in, host_out = host_out, host_in
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": world * C * K_e2e / e2e_s, "unit": METRIC, "h2d_bytes_per_step": C * 16,
+           "d2h_bytes_per_step": C * 16}
+
+    # roofline of the dominant kernel (algorithmic bytes / event time)
+    cg_bytes = sum(perfmodel.cg_bytes(C, W, int(k)) for k in k_p)
+    bi_bytes = sum(perfmodel.bicgstab_bytes(C, W, int(k)) for k in k_u)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    if cg_ms.sum() >= bicg_ms.sum():
+        kname, kbytes, kms, nl = "cg_kernel", cg_bytes, cg_ms.sum(), K_
+    else:
+        kname, kbytes, kms, nl = "bicgstab_kernel", bi_bytes, bicg_ms.sum(), K_
+    achieved = kbytes / (kms * 1e-3) / 1e9
+    step_bytes = [perfmodel.simple_step_bytes(C, K, Ki, B, F, W, int(a), int(b))["total"] for a, b in zip(k_u, k_p)]
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K_, "warmup": args.warmup,
+        "ms_per_step": total_ms / K_, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOADS[args.workload], "cells": C, "faces": K, "l2": "flushed between steps "
+                   "(256 MiB write outside the step events)", "parallelism": f"replicas x{world}",
+                   "krylov_iters_mean": {"bicgstab": float(k_u.mean()), "cg": float(k_p.mean())}},
+        "e2e": e2e,
+        "gpu_launches": 13 * K_,
+        "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks
+                     else "fallback", "traffic": None,
+                     "bytes_per_launch": kbytes / nl, "ms_per_launch": kms / nl,
+                     "step_bytes_per_s_GBs": float(np.sum(step_bytes) / (total_ms * 1e-3) / 1e9)},
+        "kernel_ms": {"bicgstab": float(bicg_ms.mean()), "cg": float(cg_ms.mean()), "step": float(step_ms.mean())},
+    }
+    if rank == 0:
+        line["clocks"] = clocks.summary()
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(args.workload, mesh, seconds=args.cpu_seconds)
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="channel", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-seconds", type=float, default=150.0)
+    ap.add_argument("--no-clocks", action="store_true", help="do not sample nvidia-smi during the timed region")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

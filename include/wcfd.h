@@ -97,15 +97,17 @@ typedef struct wcfd_system {
     int32_t pad_;
 } wcfd_system;
 
+#define WCFD_MAX_BLOCKS 2048
+#define WCFD_BARRIER_WORDS (WCFD_MAX_BLOCKS + 4)
+
 /* Krylov workspace (caller-allocated, see wcfd_krylov_workspace_floats) */
 typedef struct wcfd_krylov_ws {
-    float*    vec;        /* wcfd_krylov_workspace_floats(C, ncomp) floats        */
-    double*   partials;   /* 8 * WCFD_MAX_BLOCKS doubles                          */
-    double*   results;    /* 8 doubles                                            */
-    uint32_t* barrier;    /* 4 words: count, generation, error; the call zeroes them */
+    float*    vec;        /* wcfd_krylov_workspace_floats(C, ncomp) floats            */
+    double*   partials;   /* 8 * WCFD_MAX_BLOCKS doubles (reduction partials)         */
+    double*   results;    /* unused, may be NULL                                      */
+    uint32_t* barrier;    /* WCFD_BARRIER_WORDS words: per-block arrival flags, then the
+                             error word; every solve call zeroes them first           */
 } wcfd_krylov_ws;
-
-#define WCFD_MAX_BLOCKS 2048
 
 typedef struct wcfd_solve_stats {
     int32_t iterations;
@@ -147,6 +149,8 @@ typedef struct wcfd_case {
     wcfd_krylov_ws ws_p;       /* pressure workspace (ncomp 1)                        */
     wcfd_solve_stats* stats;   /* [2]: [0] momentum, [1] pressure (last corrector)    */
     wcfd_params    prm;
+    void* const*   events;     /* optional host array of 4 cudaEvent_t recorded before/after the
+                                  momentum solve and before/after the last pressure solve; NULL = none */
 } wcfd_case;
 
 /* ------------------------------------------------------------------ info */

@@ -1,0 +1,64 @@
+"""Converged-state comparison of the GPU drop-in with the oracle's golden fixtures
+(tests/golden/make_golden.py).
+
+At the reference's own Krylov tolerance (atol 1e-5, fp32) the outer-iteration
+trajectory depends on rounding: two oracle runs of the same method, fp32 and fp64,
+differ by ~2e-3 (u, v) and ~1e-1 (p) after 500 iterations of the 64x64 cavity.  So:
+  * converged state, tightened atol (1e-7 both solvers): GPU fp32 vs the fp64 oracle
+    fixture within 5e-5 (u, v; measured on the velocity norm) and 2e-3 (p), the
+    fp32 floor of this problem;
+  * the reference's own settings: GPU vs the fp32 oracle fixture within three times the
+    oracle's own fp32-vs-fp64 spread.
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from tests.cases import cavity_bc, cavity_mesh
+from tests.gpu_helpers import fields, make_pair, rel_l2, vel_err
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib_ready():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from warpcfd_gb300.build import build_library
+    build_library()
+
+
+def _run(n_iter, atol):
+    m = cavity_mesh(64)
+    model, solver, _ = make_pair(m, cavity_bc, atol=atol)
+    solver.set_iterations(n_iter, 1, 1)
+    solver.run(steps_per_check=0, use_cuda_graph=True)
+    return fields(model)
+
+
+def test_converged_cavity_matches_fp64_fixture():
+    fx = np.load(os.path.join(GOLDEN, "ldc64_fp64_converged.npz"))["cell_values"]
+    g = _run(1500, 1e-7)
+    eu, ev, ep = vel_err(g, fx, 0), vel_err(g, fx, 1), rel_l2(g[:, 3], fx[:, 3])
+    print(f"converged 64x64 cavity vs fp64 oracle: u {eu:.2e} v {ev:.2e} p {ep:.2e}")
+    assert eu < 5e-5 and ev < 5e-5
+    assert ep < 2e-3
+    assert np.abs(g[:, 2]).max() == 0.0
+
+
+def test_reference_settings_within_oracle_spread():
+    f32 = np.load(os.path.join(GOLDEN, "ldc64_fp32_500.npz"))["cell_values"]
+    f64 = np.load(os.path.join(GOLDEN, "ldc64_fp64_500.npz"))["cell_values"]
+    g = _run(500, 1e-5)
+    for o in (0, 1):
+        spread = vel_err(f32, f64, o)
+        got = vel_err(g, f32, o)
+        print(f"field {o}: gpu vs oracle fp32 {got:.2e}, oracle fp32 vs fp64 {spread:.2e}")
+        assert got < 3 * spread + 1e-5
+    spread_p = rel_l2(f32[:, 3], f64[:, 3])
+    got_p = rel_l2(g[:, 3], f32[:, 3])
+    print(f"p: gpu vs oracle fp32 {got_p:.2e}, oracle fp32 vs fp64 {spread_p:.2e}")
+    assert got_p < 3 * spread_p + 1e-4

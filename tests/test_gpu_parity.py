@@ -1,0 +1,189 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle on the same seeded inputs.
+
+Tolerances (relative L2; a velocity component is measured against the norm of the whole
+velocity field, p against its own norm; fp32 arithmetic on both sides, so the only
+differences are summation order and fma contraction):
+  single operators ............... 1e-5 (faces/gradients), 1e-5 (assembled matrices)
+  one SIMPLE/PISO step ........... 1e-5 (u, v, w), 1e-4 (p)
+  5-step trajectory .............. 1e-4 (u, v, w), 1e-3 (p)
+The fixed-iteration-count comparison at the reference's own Krylov tolerance is
+path-dependent (see test_gpu_converged.py for the converged comparison).
+"""
+import numpy as np
+import pytest
+import torch
+
+from tests.cases import cavity3d_bc, cavity3d_mesh, cavity_bc, cavity_mesh, channel_bc, channel_mesh
+from tests.gpu_helpers import fields, make_pair, oracle_step, rel_l2, vel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib_ready():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from warpcfd_gb300.build import build_library
+    build_library()
+
+
+def _seed_state(model, oc, seed):
+    rng = np.random.default_rng(seed)
+    C = model.num_cells
+    cv = rng.uniform(-1, 1, size=(C, 4)).astype(np.float32)
+    cg = rng.uniform(-1, 1, size=(C, 4, 3)).astype(np.float32)
+    model.cell_values.copy_(torch.from_numpy(cv))
+    model.cell_gradients.copy_(torch.from_numpy(cg))
+    oc.cell_values[:] = cv
+    oc.cell_gradients[:] = cg
+
+
+@pytest.mark.parametrize("jitter", [0.0, 0.15])
+def test_face_pass_gradients_flux_div(jitter):
+    m = cavity_mesh(12, jitter=jitter, seed=5)
+    model, solver, oc = make_pair(m, cavity_bc)
+    _seed_state(model, oc, 1)
+    model.set_boundary_conditions()
+    model.face_interpolation()
+    oc.apply_bc()
+    oc.face_interpolation()
+    fv = model.face_values.cpu().numpy()
+    for o in range(4):
+        assert rel_l2(fv[:, o], oc.face_values[:, o]) < 1e-6
+    model.calculate_gradients()
+    oc.calculate_gradients()
+    g = model.cell_gradients.cpu().numpy()
+    assert rel_l2(g, oc.cell_gradients) < 1e-5
+    model.calculate_mass_flux()
+    oc.calculate_mass_flux()
+    assert rel_l2(model.mass_fluxes.cpu().numpy(), oc.mass_fluxes) < 1e-6
+    d = model.divFlux().cpu().numpy()
+    assert np.abs(d - oc.div_flux()).max() <= 1e-5 * np.abs(oc.mass_fluxes).max()
+    # p-only gradient zeroes every other field (model.py:237)
+    model.calculate_gradients("p")
+    g = model.cell_gradients.cpu().numpy()
+    assert np.abs(g[:, :3]).max() == 0.0 and np.abs(g[:, 3]).max() > 0
+
+
+def test_upwind_face_interpolation():
+    m = cavity_mesh(8, jitter=0.1, seed=2)
+    model, solver, oc = make_pair(m, cavity_bc)
+    _seed_state(model, oc, 2)
+    mf = np.random.default_rng(3).standard_normal(m.num_faces).astype(np.float32)
+    model.mass_fluxes.copy_(torch.from_numpy(mf))
+    model.face_interpolation(upwind=True)
+    fv = model.face_values.cpu().numpy()
+    fp = m.face_properties
+    ii = fp.internal_face_ids
+    P, N = fp.adjacent_cells[ii, 0], fp.adjacent_cells[ii, 1]
+    up = np.where(mf[ii] > 0, P, N)
+    oc.face_interpolation()  # skew term of the linear scheme = same skew correction
+    lin = oc.cell_values[P] * oc.g.psi[ii, None] + oc.g.psi2[ii, None] * oc.cell_values[N]
+    skew = oc.face_values[ii] - lin
+    np.testing.assert_allclose(fv[ii], oc.cell_values[up] + skew, rtol=1e-5, atol=1e-6)
+
+
+@pytest.mark.parametrize("case", ["cavity", "channel", "cavity3d"])
+def test_assembly_matches_oracle(case):
+    mk = {"cavity": (lambda: cavity_mesh(10, jitter=0.1, seed=1), cavity_bc, 0),
+          "channel": (lambda: channel_mesh(20, 5), channel_bc, None),
+          "cavity3d": (lambda: cavity3d_mesh(5), cavity3d_bc, 0)}[case]
+    m = mk[0]()
+    model, solver, oc = make_pair(m, mk[1], ref_cell=mk[2])
+    _seed_state(model, oc, 4)
+    # the face pass of an outer iteration, on both sides
+    model.set_boundary_conditions()
+    model.face_interpolation()
+    model.calculate_gradients()
+    model.calculate_mass_flux()
+    oc.apply_bc()
+    oc.face_interpolation()
+    oc.calculate_gradients()
+    oc.calculate_mass_flux()
+    solver.assemble_momentum()
+    wc = oc.convection_weights()
+    wd = oc.diffusion_weights((0, 1, 2), 0.01)
+    vals, rhs = oc.assemble(3, [(wc, 1.0), (wd, -1.0)], (), [(oc.grad_term(), -1.0)])
+    oc.relax(vals, rhs, 0.7, (0, 1, 2))
+    A_ref = oc.momentum_matrix(vals).toarray()
+    A_gpu = solver.vel_equation.dense.cpu().numpy()
+    assert rel_l2(A_gpu, A_ref) < 1e-5
+    assert rel_l2(solver.vel_equation.rhs.cpu().numpy(), rhs.reshape(-1)) < 1e-5
+    rua_ref = oc.g.volume / (vals[0, oc.diag_pos] * np.float32(1.0))
+    assert rel_l2(solver.rUA.cpu().numpy(), rua_ref) < 1e-5
+    # pressure system with rUA_f and div from the same state
+    rua_f = np.random.default_rng(5).uniform(0.1, 1.0, size=m.num_faces).astype(np.float32)
+    solver.rUA_faces.copy_(torch.from_numpy(rua_f))
+    div = oc.div_flux()
+    solver.div_u.copy_(torch.from_numpy(div))
+    solver.assemble_pressure()
+    wpd = oc.diffusion_weights((3,), rua_f)
+    pv, prhs = oc.assemble(1, [(wpd, 1.0)])
+    prhs[:, 0] += div
+    if mk[2] is not None:
+        rc = mk[2]
+        s, e = oc.indptr[rc], oc.indptr[rc + 1]
+        pv[0, s:e] = np.where(oc.pat_cols[s:e] == rc, 1.0, 0.0)
+        prhs[rc, 0] = 0.0
+    assert rel_l2(solver.p_corr_equation.dense.cpu().numpy(), oc.matrix(pv[0]).toarray()) < 1e-5
+    assert rel_l2(solver.p_corr_equation.rhs.cpu().numpy(), prhs[:, 0]) < 1e-5
+
+
+@pytest.mark.parametrize("case", ["cavity", "cavity_skew", "channel", "cavity3d"])
+def test_simple_steps_track_oracle(case):
+    mk = {"cavity": (lambda: cavity_mesh(24), cavity_bc, 0, 0.01),
+          "cavity_skew": (lambda: cavity_mesh(16, jitter=0.15, seed=11), cavity_bc, 0, 0.01),
+          "channel": (lambda: channel_mesh(40, 8), channel_bc, None, 0.05),
+          "cavity3d": (lambda: cavity3d_mesh(8), cavity3d_bc, 0, 0.01)}[case]
+    m = mk[0]()
+    model, solver, oc = make_pair(m, mk[1], ref_cell=mk[2], nu=mk[3])
+    for it in range(5):
+        solver.step()
+        oracle_step(oc)
+        g = fields(model)
+        st = solver.solve_stats()
+        tol_u = 1e-5 if it == 0 else 1e-4
+        tol_p = 1e-4 if it == 0 else 1e-3
+        for o in range(3):
+            assert vel_err(g, oc.cell_values, o) < tol_u, (it, o)
+        assert rel_l2(g[:, 3], oc.cell_values[:, 3]) < tol_p, it
+        assert st[0]["status"] in ("ok", "not converged") and st[1]["status"] in ("ok", "not converged")
+        # the GPU needs the same number of Krylov iterations (+-2 near the stop boundary)
+        assert abs(st[0]["iterations"] - oc.log[-1][0]) <= 2
+        assert abs(st[1]["iterations"] - oc.log[-1][2]) <= 2
+
+
+def test_piso_steps_track_oracle():
+    m = cavity_mesh(20, jitter=0.1, seed=3)
+    model, solver, oc = make_pair(m, cavity_bc, steady=False, dt=0.01, inner=2)
+    for it in range(4):
+        solver.step()
+        oracle_step(oc, None, None, steady=False, dt=0.01, inner=2)
+        g = fields(model)
+        for o in (0, 1):
+            assert vel_err(g, oc.cell_values, o) < 1e-4, (it, o)
+        assert rel_l2(g[:, 3], oc.cell_values[:, 3]) < 1e-3, it
+
+
+def test_cuda_graph_replay_is_bitwise_identical():
+    m = cavity_mesh(16)
+    model_a, solver_a, _ = make_pair(m, cavity_bc)
+    model_b, solver_b, _ = make_pair(m, cavity_bc)
+    for _ in range(4):
+        solver_a.step()
+    solver_b.run(steps_per_check=0, use_cuda_graph=True)   # 1 outer loop: eager first step
+    for _ in range(3):
+        solver_b._graph_step_counted()
+    torch.cuda.synchronize()
+    assert torch.equal(model_a.cell_values, model_b.cell_values)
+
+
+def test_runs_are_bitwise_reproducible():
+    m = cavity_mesh(20, jitter=0.1, seed=1)
+    outs = []
+    for _ in range(2):
+        model, solver, _ = make_pair(m, cavity_bc)
+        for _ in range(3):
+            solver.step()
+        outs.append(fields(model))
+    assert np.array_equal(outs[0], outs[1])

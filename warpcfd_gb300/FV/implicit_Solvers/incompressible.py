@@ -58,6 +58,18 @@ class IncompressibleSolver:
         self._graph = None
         self._graph_key = None
         self._mesh_t = model.mesh_struct(correction=correction)
+        self._events = None
+        self._events_ptr = None
+
+    def set_timing_events(self, events):
+        """Record 4 torch.cuda.Events (already recorded once, so they exist) around the
+        momentum solve and the last pressure solve of every step; None to stop."""
+        if events is None:
+            self._events, self._events_ptr = None, None
+            return
+        arr = (ct.c_void_p * 4)(*[ct.c_void_p(e.cuda_event) for e in events])
+        self._events = (events, arr)
+        self._events_ptr = ct.cast(arr, ct.c_void_p)
 
     def set_time_stepping(self, MAX_TIME_STEPS, dt, automatic=False, CFL_Max=1.0):
         if automatic is not False:
@@ -91,13 +103,23 @@ class IncompressibleSolver:
         return _lib.Case_t(self._mesh_t, m.bc_struct(), m.state_struct(), ve.system_struct(), pe.system_struct(),
                            self.HbyA.data_ptr(), pe.x.data_ptr(), self.rUA.data_ptr(), self.rUA_faces.data_ptr(),
                            self.div_u.data_ptr(), ve.workspace_struct(), pe.workspace_struct(),
-                           self.stats.data_ptr(), self.params())
+                           self.stats.data_ptr(), self.params(), self._events_ptr)
 
     # ------------------------------------------------------------------ stepping
     def step(self):
         """One SIMPLE outer iteration or one PISO time step on the current stream."""
         case = self.case_struct()
         _lib.call("wcfd_simple_iteration", ct.byref(case), _stream())
+
+    def assemble_momentum(self):
+        """Momentum system from the current fields (incompressible.py:102-113) into
+        vel_equation.diag/off/rhs, and rUA."""
+        _lib.call("wcfd_assemble_momentum", ct.byref(self.case_struct()), _stream())
+
+    def assemble_pressure(self):
+        """Pressure system from rUA_faces and div_u (incompressible.py:134-140) into
+        p_corr_equation.diag/off/rhs."""
+        _lib.call("wcfd_assemble_pressure", ct.byref(self.case_struct()), _stream())
 
     def solve_stats(self):
         """(momentum, pressure) Krylov outcomes of the last step: iterations, status, residual."""

@@ -60,7 +60,7 @@ class Equation:
         self.ws_vec = torch.zeros(nws, **f32)
         self.ws_partials = torch.zeros(8 * _lib.MAX_BLOCKS, dtype=torch.float64, device=dev)
         self.ws_results = torch.zeros(8, dtype=torch.float64, device=dev)
-        self.ws_barrier = torch.zeros(4, dtype=torch.int32, device=dev)
+        self.ws_barrier = torch.zeros(_lib.BARRIER_WORDS, dtype=torch.int32, device=dev)
         self.stats = torch.zeros(16, dtype=torch.uint8, device=dev)
 
     @property

@@ -24,6 +24,7 @@ STATUS_NAMES = {0: "ok", 1: "bad argument", 2: "cuda error", 3: "krylov breakdow
 
 WCFD_U, WCFD_V, WCFD_W, WCFD_P, WCFD_ALL = 1, 2, 4, 8, 15
 MAX_BLOCKS = 2048
+BARRIER_WORDS = MAX_BLOCKS + 4
 
 vp = ct.c_void_p
 
@@ -67,7 +68,8 @@ class Params_t(ct.Structure):
 class Case_t(ct.Structure):
     _fields_ = [("mesh", Mesh_t), ("bc", BC_t), ("state", State_t), ("mom", System_t), ("pres", System_t),
                 ("hbya", vp), ("p_x", vp), ("rua", vp), ("rua_faces", vp), ("div", vp),
-                ("ws_u", KrylovWS_t), ("ws_p", KrylovWS_t), ("stats", vp), ("prm", Params_t)]
+                ("ws_u", KrylovWS_t), ("ws_p", KrylovWS_t), ("stats", vp), ("prm", Params_t),
+                ("events", vp)]
 
 
 # name -> (restype, argtypes)

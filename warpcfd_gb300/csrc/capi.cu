@@ -77,7 +77,7 @@ int launch_krylov(const void* fn, int slot, const wcfd_mesh* m, wcfd_system A, f
                   double atol, int maxiter, wcfd_solve_stats* stats, cudaStream_t st, const char* name) {
     int rc = check_mesh(m);
     if (rc) return rc;
-    RET_IF(!A.diag || !A.off || !A.rhs || !x || !ws.vec || !ws.partials || !ws.results || !ws.barrier || !stats,
+    RET_IF(!A.diag || !A.off || !A.rhs || !x || !ws.vec || !ws.partials || !ws.barrier || !stats,
            WCFD_ERR_ARGUMENT, "null solver argument");
     RET_IF(maxiter < 0 || !(atol >= 0.0), WCFD_ERR_ARGUMENT, "bad atol or maxiter");
     const int cap = coop_capacity(fn, slot);
@@ -86,7 +86,7 @@ int launch_krylov(const void* fn, int slot, const wcfd_mesh* m, wcfd_system A, f
     long long want = (m->n_cells + kSolverBlock - 1) / kSolverBlock;
     int grid = (int)(want < cap ? want : cap);
     if (grid < 1) grid = 1;
-    if (cudaMemsetAsync(ws.barrier, 0, 4 * sizeof(uint32_t), st) != cudaSuccess)
+    if (cudaMemsetAsync(ws.barrier, 0, WCFD_BARRIER_WORDS * sizeof(uint32_t), st) != cudaSuccess)
         return set_error(WCFD_ERR_CUDA, "barrier reset failed");
     KrylovArgs a;
     a.m = *m;
@@ -94,9 +94,8 @@ int launch_krylov(const void* fn, int slot, const wcfd_mesh* m, wcfd_system A, f
     a.x = x;
     a.ws = ws.vec;
     a.g.partials = ws.partials;
-    a.g.results = ws.results;
-    a.g.bar = ws.barrier;
-    a.g.err = reinterpret_cast<int*>(ws.barrier + 2);
+    a.g.flags = ws.barrier;
+    a.g.err = reinterpret_cast<int*>(ws.barrier + WCFD_MAX_BLOCKS);
     a.atol2 = atol * atol;
     a.maxiter = maxiter;
     a.stats = stats;
@@ -120,7 +119,7 @@ const char* wcfd_last_error(void) { return g_last_error; }
 
 int64_t wcfd_krylov_workspace_floats(int32_t n_cells, int32_t ncomp) {
     if (n_cells <= 0 || (ncomp != 1 && ncomp != 3)) return -1;
-    return ncomp == 1 ? 4LL * n_cells : 18LL * n_cells;
+    return ncomp == 1 ? 5LL * n_cells : 27LL * n_cells;
 }
 
 int wcfd_face_pass_flags(const wcfd_mesh* m, wcfd_bc bc, wcfd_state s, uint32_t mask, uint32_t flags,
@@ -249,8 +248,13 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
     // :102-116
     rc = wcfd_assemble_momentum(cp, stream);
     if (rc) return rc;
+    auto mark = [&](int i) {
+        if (c.events && c.events[i]) cudaEventRecord(reinterpret_cast<cudaEvent_t>(c.events[i]), st);
+    };
+    mark(0);
     rc = wcfd_bicgstab(&m, c.mom, c.hbya, c.ws_u, c.prm.atol_u, c.prm.maxiter, c.stats + 0, stream);
     if (rc) return rc;
+    mark(1);
     // :118-123
     hbya_kernel<<<gc, kBlock, 0, st>>>(m.n_cells, c.state.cell_gradients, c.rua, c.hbya, c.state.cell_values);
     LAUNCH_CHECK("hbya_kernel");
@@ -266,8 +270,11 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
             // :134-142
             rc = wcfd_assemble_pressure(cp, stream);
             if (rc) return rc;
+            const bool last = inner == c.prm.n_inner - 1 && ortho == c.prm.n_ortho - 1;
+            if (last) mark(2);
             rc = wcfd_cg(&m, c.pres, c.p_x, c.ws_p, c.prm.atol_p, c.prm.maxiter, c.stats + 1, stream);
             if (rc) return rc;
+            if (last) mark(3);
             // :144-147
             p_update_kernel<<<gc, kBlock, 0, st>>>(m.n_cells, c.p_x, c.state.cell_values,
                                                    c.prm.steady ? c.prm.p_relax : 0.0f);

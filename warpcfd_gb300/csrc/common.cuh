@@ -64,91 +64,73 @@ __device__ __forceinline__ void block_sum(double (&v)[NV]) {
 }
 
 // Grid-wide synchronisation state living in caller-provided global memory.
+//   flags[b]   phase number block b has reached (zeroed before each launch)
+//   partials   [2 phase parities][4 values][WCFD_MAX_BLOCKS] per-block partial sums
 struct GridCtl {
-    double* partials;   // [8][WCFD_MAX_BLOCKS]
-    double* results;    // [8]
-    unsigned* bar;      // [0] arrival count, [1] generation
-    int* err;           // status word shared by all blocks of the launch
+    double* partials;
+    unsigned* flags;
+    int* err;
 };
 
-// Barrier over all blocks of a cooperative launch.  When NV > 0 the last block to
-// arrive sums the NV per-block partials (v[] of every block) in block-index order, so
-// every run and every block gets the same bits, and publishes them in results[] before
-// releasing the others; on return v[] holds the grid-wide sums.  Every wait is bounded:
-// on timeout the block sets *err and returns false, as it does when another block has
-// already flagged an error.
+// Barrier + reduction over all blocks of a cooperative launch, for phase number `phase`
+// (1, 2, 3, ... in every block).  Each block publishes its NV partial sums and then its
+// flag with one release store (no atomics); every block waits for all flags (one thread
+// per flag, in parallel) and sums the partials in block-index order, so every block gets
+// the same bits on every run.  Partials are double-buffered by phase parity: a block can
+// only overwrite a buffer after every block has passed the phase that read it.
+// Every wait is bounded: on timeout the block sets *err and returns false.
 template <int NV, int BS>
-__device__ bool grid_sync(const GridCtl& g, double* v) {
-    __shared__ int s_last, s_fail;
-    __shared__ unsigned s_gen;
+__device__ bool grid_sync(const GridCtl& g, double* v, unsigned phase) {
+    __shared__ int s_fail;
+    if (threadIdx.x == 0) s_fail = 0;
     if constexpr (NV > 0) {
         double t[NV];
 #pragma unroll
         for (int i = 0; i < NV; ++i) t[i] = v[i];
         block_sum<NV, BS>(t);
         if (threadIdx.x == 0) {
+            double* pb = g.partials + (size_t)(phase & 1u) * 4 * WCFD_MAX_BLOCKS;
 #pragma unroll
-            for (int i = 0; i < NV; ++i) g.partials[i * WCFD_MAX_BLOCKS + blockIdx.x] = t[i];
+            for (int i = 0; i < NV; ++i) pb[i * WCFD_MAX_BLOCKS + blockIdx.x] = t[i];
         }
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        s_fail = 0;
-        const unsigned gen = ld_acquire(g.bar + 1);
-        s_gen = gen;
-        __threadfence();
-        const unsigned prev = atomicAdd(g.bar, 1u);
-        s_last = (prev == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (s_last) {
-        __threadfence();
+    __syncthreads();  // this block's writes of the phase happen before its release
+    if (threadIdx.x == 0) st_release(g.flags + blockIdx.x, phase);
+    double acc[NV > 0 ? NV : 1];
+#pragma unroll
+    for (int i = 0; i < (NV > 0 ? NV : 1); ++i) acc[i] = 0.0;
+    bool ok = true;
+    for (int j = threadIdx.x; j < (int)gridDim.x; j += BS) {
+        if ((int)(ld_acquire(g.flags + j) - phase) < 0) {
+            const uint64_t t0 = global_ns();
+            unsigned spins = 0;
+            while ((int)(ld_acquire(g.flags + j) - phase) < 0) {
+                if ((++spins & 31u) == 0u && global_ns() - t0 > kBarrierTimeoutNs) {
+                    ok = false;
+                    break;
+                }
+                __nanosleep(20);
+            }
+        }
+        if (!ok) break;
         if constexpr (NV > 0) {
-            double acc[NV];
+            const double* pb = g.partials + (size_t)(phase & 1u) * 4 * WCFD_MAX_BLOCKS;
 #pragma unroll
-            for (int i = 0; i < NV; ++i) {
-                double a = 0.0;
-                for (int b = threadIdx.x; b < (int)gridDim.x; b += BS)
-                    a += __ldcg(g.partials + i * WCFD_MAX_BLOCKS + b);
-                acc[i] = a;
-            }
-            block_sum<NV, BS>(acc);
-            if (threadIdx.x == 0) {
-#pragma unroll
-                for (int i = 0; i < NV; ++i) g.results[i] = acc[i];
-            }
-            __threadfence();
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            atomicExch(g.bar, 0u);
-            __threadfence();
-            st_release(g.bar + 1, s_gen + 1u);
-        }
-    } else if (threadIdx.x == 0) {
-        const uint64_t t0 = global_ns();
-        unsigned spins = 0;
-        while (ld_acquire(g.bar + 1) == s_gen) {
-            if ((++spins & 63u) == 0u && global_ns() - t0 > kBarrierTimeoutNs) {
-                atomicExch(g.err, WCFD_BARRIER_TIMEOUT);
-                s_fail = 1;
-                break;
-            }
-            __nanosleep(32);
+            for (int i = 0; i < NV; ++i) acc[i] += __ldcg(pb + i * WCFD_MAX_BLOCKS + j);
         }
     }
-    __syncthreads();
-    __threadfence();
-    if (threadIdx.x == 0 && !s_fail) {
-        if (*((volatile int*)g.err) != 0) s_fail = 1;
+    if (!ok) {
+        atomicExch(g.err, WCFD_BARRIER_TIMEOUT);
+        s_fail = 1;
     }
-    __syncthreads();
-    if (s_fail) return false;
     if constexpr (NV > 0) {
+        block_sum<NV, BS>(acc);  // contains __syncthreads, so s_fail is visible after it
 #pragma unroll
-        for (int i = 0; i < NV; ++i) v[i] = __ldcg(g.results + i);
+        for (int i = 0; i < NV; ++i) v[i] = acc[i];
+    } else {
+        __syncthreads();
     }
-    return true;
+    return s_fail == 0;
 }
 
 }  // namespace wcfd

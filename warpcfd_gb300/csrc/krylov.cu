@@ -4,35 +4,18 @@
 // with the diagonal (Jacobi) preconditioner as called by Equation.solve_Axb
 // (warp_cfd/FV/terms/equation.py:195-200).  Stop test: ||r||_2 <= atol before an
 // iteration, or maxiter iterations.
+//
+// Each search-direction update (CG: p = z + beta p; BiCGSTAB: p = r + beta (p - omega v),
+// s = r - alpha v) is evaluated on the fly inside the SpMV that consumes it, for the row
+// itself and for every gathered neighbour, and the new direction is written to the other
+// half of a double buffer.  The arithmetic is the textbook algorithm's, but a CG iteration
+// needs two grid barriers instead of three and a BiCGSTAB iteration three instead of five.
 #include "common.cuh"
 #include "kernels.cuh"
 
 namespace wcfd {
 
 constexpr int BS = kSolverBlock;
-
-// sum_j A_ij (w_j x_j) for the NC components of row i; w = nullptr means w = 1.
-template <int NC>
-__device__ __forceinline__ void row_apply(const KrylovArgs& a, int i, const float* __restrict__ x,
-                                          const float* __restrict__ w, float (&out)[NC]) {
-    const int C = a.m.n_cells;
-#pragma unroll
-    for (int o = 0; o < NC; ++o) {
-        const size_t q = NC * (size_t)i + o;
-        const float xi = w ? x[q] * w[q] : x[q];
-        out[o] = a.A.diag[q] * xi;
-    }
-    for (int j = 0; j < a.m.ell_width; ++j) {
-        const float v = a.A.off[(size_t)j * C + i];
-        const int col = __ldg(a.m.ell_col + (size_t)j * C + i);
-#pragma unroll
-        for (int o = 0; o < NC; ++o) {
-            const size_t q = NC * (size_t)col + o;
-            const float xj = w ? x[q] * w[q] : x[q];
-            out[o] += v * xj;
-        }
-    }
-}
 
 __device__ __forceinline__ float jacobi(float d) { return d != 0.0f ? 1.0f / d : 1.0f; }
 
@@ -48,7 +31,7 @@ __device__ void fail_stats(const KrylovArgs& a, int k) {
 
 #define SYNC(NV, arr)                                   \
     do {                                                \
-        if (!grid_sync<NV, BS>(a.g, arr)) {             \
+        if (!grid_sync<NV, BS>(a.g, arr, ++phase)) {    \
             fail_stats(a, k);                           \
             return;                                     \
         }                                               \
@@ -64,50 +47,67 @@ __device__ void write_stats(const KrylovArgs& a, int k, double rr, int status) {
     }
 }
 
-// Jacobi-preconditioned CG (scalar system).  Workspace: r, p, q, invd (4 C floats).
+// Jacobi-preconditioned CG on a scalar system.
+// Workspace: r, pA, pB, q, invd (5 C floats).
 __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
     const int C = a.m.n_cells;
+    const int W = a.m.ell_width;
     float* r = a.ws;
-    float* p = a.ws + (size_t)C;
-    float* q = a.ws + 2 * (size_t)C;
-    float* invd = a.ws + 3 * (size_t)C;
-    const float* b = a.A.rhs;
+    float* pbuf[2] = {a.ws + (size_t)C, a.ws + 2 * (size_t)C};
+    float* q = a.ws + 3 * (size_t)C;
+    float* invd = a.ws + 4 * (size_t)C;
+    const float* __restrict__ b = a.A.rhs;
+    const float* __restrict__ diag = a.A.diag;
+    const float* __restrict__ off = a.A.off;
+    const int* __restrict__ col = a.m.ell_col;
     float* x = a.x;
     const int stride = gridDim.x * BS;
     const int i0 = blockIdx.x * BS + threadIdx.x;
+    unsigned phase = 0;
+    int k = 0, status = WCFD_OK;
 
     // r = b - A x ; z = M r ; p = z ; rr = r.r ; rz = r.z
     double red[2] = {0.0, 0.0};
     for (int i = i0; i < C; i += stride) {
-        float ax[1];
-        row_apply<1>(a, i, x, nullptr, ax);
-        const float ri = b[i] - ax[0];
-        const float di = jacobi(a.A.diag[i]);
+        float ax = diag[i] * x[i];
+        for (int j = 0; j < W; ++j) ax += off[(size_t)j * C + i] * x[col[(size_t)j * C + i]];
+        const float ri = b[i] - ax;
+        const float di = jacobi(diag[i]);
         const float zi = ri * di;
         r[i] = ri;
         invd[i] = di;
-        p[i] = zi;
+        pbuf[0][i] = zi;
         red[0] += (double)ri * ri;
         red[1] += (double)ri * zi;
     }
-    int k = 0, status = WCFD_OK;
     SYNC(2, red);
     double rr = red[0], rz = red[1];
+    float bf = 0.0f;  // first direction is z itself
+    int cur = 0;
     while (k < a.maxiter && rr > a.atol2) {
+        const float* po = pbuf[cur];  // written by other blocks in this launch: no restrict
+        float* pn = pbuf[cur ^ 1];
+        // p_new = z + beta p_old (here and for every neighbour) ; q = A p_new ; p.q
         double pq[1] = {0.0};
         for (int i = i0; i < C; i += stride) {
-            float qi[1];
-            row_apply<1>(a, i, p, nullptr, qi);
-            q[i] = qi[0];
-            pq[0] += (double)p[i] * qi[0];
+            const float pi = r[i] * invd[i] + bf * po[i];
+            float qi = diag[i] * pi;
+            for (int j = 0; j < W; ++j) {
+                const int c = col[(size_t)j * C + i];
+                qi += off[(size_t)j * C + i] * (r[c] * invd[c] + bf * po[c]);
+            }
+            pn[i] = pi;
+            q[i] = qi;
+            pq[0] += (double)pi * qi;
         }
         SYNC(1, pq);
         if (pq[0] == 0.0) { status = WCFD_KRYLOV_BREAKDOWN; break; }
         const double alpha = rz / pq[0];
         const float af = (float)alpha;
+        // x += alpha p ; r -= alpha q ; rr ; rz
         double red2[2] = {0.0, 0.0};
         for (int i = i0; i < C; i += stride) {
-            x[i] += af * p[i];
+            x[i] += af * pn[i];
             const float ri = r[i] - af * q[i];
             r[i] = ri;
             const float zi = ri * invd[i];
@@ -118,59 +118,96 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
         rr = red2[0];
         const double beta = rz != 0.0 ? red2[1] / rz : 0.0;
         rz = red2[1];
-        const float bf = (float)beta;
-        for (int i = i0; i < C; i += stride) p[i] = r[i] * invd[i] + bf * p[i];
-        SYNC(0, nullptr);
+        bf = (float)beta;
+        cur ^= 1;
         ++k;
     }
     write_stats(a, k, rr, status);
 }
 
-// Right-preconditioned (Jacobi) BiCGSTAB on the 3-component momentum system.
-// Workspace: r, r0, p, v, t, invd (6 x 3C floats).  s overwrites r.
+// Right-preconditioned (Jacobi) BiCGSTAB on the 3-component momentum system
+// (interleaved rows 3c+o, shared off-diagonals).
+// Workspace (3C floats each): r, r0, pA, pB, vA, vB, t, s, invd.
 __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
     const int C = a.m.n_cells;
+    const int W = a.m.ell_width;
     const size_t n3 = 3 * (size_t)C;
     float* r = a.ws;
     float* r0 = a.ws + n3;
-    float* p = a.ws + 2 * n3;
-    float* v = a.ws + 3 * n3;
-    float* t = a.ws + 4 * n3;
-    float* invd = a.ws + 5 * n3;
-    const float* b = a.A.rhs;
+    float* pbuf[2] = {a.ws + 2 * n3, a.ws + 3 * n3};
+    float* vbuf[2] = {a.ws + 4 * n3, a.ws + 5 * n3};
+    float* t = a.ws + 6 * n3;
+    float* s = a.ws + 7 * n3;
+    float* invd = a.ws + 8 * n3;
+    const float* __restrict__ b = a.A.rhs;
+    const float* __restrict__ diag = a.A.diag;
+    const float* __restrict__ off = a.A.off;
+    const int* __restrict__ col = a.m.ell_col;
     float* x = a.x;
     const int stride = gridDim.x * BS;
     const int i0 = blockIdx.x * BS + threadIdx.x;
+    unsigned phase = 0;
+    int k = 0, status = WCFD_OK;
 
-    double red[2] = {0.0, 0.0};
+    // r = b - A x ; r0 = r ; p = r ; v = 0 ; rr ; rho = r0.r = rr
+    double red[1] = {0.0};
     for (int i = i0; i < C; i += stride) {
         float ax[3];
-        row_apply<3>(a, i, x, nullptr, ax);
+#pragma unroll
+        for (int o = 0; o < 3; ++o) ax[o] = diag[3 * (size_t)i + o] * x[3 * (size_t)i + o];
+        for (int j = 0; j < W; ++j) {
+            const float v = off[(size_t)j * C + i];
+            const int c = col[(size_t)j * C + i];
+#pragma unroll
+            for (int o = 0; o < 3; ++o) ax[o] += v * x[3 * (size_t)c + o];
+        }
 #pragma unroll
         for (int o = 0; o < 3; ++o) {
             const size_t q = 3 * (size_t)i + o;
             const float ri = b[q] - ax[o];
             r[q] = ri;
             r0[q] = ri;
-            p[q] = ri;
-            invd[q] = jacobi(a.A.diag[q]);
+            pbuf[0][q] = ri;
+            vbuf[0][q] = 0.0f;
+            invd[q] = jacobi(diag[q]);
             red[0] += (double)ri * ri;
         }
     }
-    int k = 0, status = WCFD_OK;
     SYNC(1, red);
     double rr = red[0];
     double rho = rr;
+    float bf = 0.0f, of = 0.0f;  // first direction is r itself
+    int cur = 0;
     while (k < a.maxiter && rr > a.atol2) {
-        // v = A (M p) ; r0.v
+        const float* po = pbuf[cur];  // written by other blocks in this launch: no restrict
+        const float* vo = vbuf[cur];
+        float* pn = pbuf[cur ^ 1];
+        float* vn = vbuf[cur ^ 1];
+        // p = r + beta (p - omega v) ; v = A (M p) ; r0.v
         double r0v[1] = {0.0};
         for (int i = i0; i < C; i += stride) {
-            float vi[3];
-            row_apply<3>(a, i, p, invd, vi);
+            float pi[3], vi[3];
 #pragma unroll
             for (int o = 0; o < 3; ++o) {
                 const size_t q = 3 * (size_t)i + o;
-                v[q] = vi[o];
+                pi[o] = r[q] + bf * (po[q] - of * vo[q]);
+                vi[o] = diag[q] * (pi[o] * invd[q]);
+            }
+            for (int j = 0; j < W; ++j) {
+                const float v = off[(size_t)j * C + i];
+                const int c = col[(size_t)j * C + i];
+#pragma unroll
+                for (int o = 0; o < 3; ++o) {
+                    const size_t q = 3 * (size_t)c + o;
+                    const float pc = r[q] + bf * (po[q] - of * vo[q]);
+                    vi[o] += v * (pc * invd[q]);
+                }
+            }
+#pragma unroll
+            for (int o = 0; o < 3; ++o) {
+                const size_t q = 3 * (size_t)i + o;
+                pn[q] = pi[o];
+                vn[q] = vi[o];
                 r0v[0] += (double)r0[q] * vi[o];
             }
         }
@@ -178,39 +215,46 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
         if (r0v[0] == 0.0) { status = WCFD_KRYLOV_BREAKDOWN; break; }
         const double alpha = rho / r0v[0];
         const float af = (float)alpha;
-        // s = r - alpha v (in r) ; x += alpha M p
-        for (int i = i0; i < C; i += stride) {
-#pragma unroll
-            for (int o = 0; o < 3; ++o) {
-                const size_t q = 3 * (size_t)i + o;
-                r[q] = r[q] - af * v[q];
-                x[q] += af * (p[q] * invd[q]);
-            }
-        }
-        SYNC(0, nullptr);
-        // t = A (M s) ; t.t ; t.s
+        // s = r - alpha v ; x += alpha M p ; t = A (M s) ; t.t ; t.s
         double ts[2] = {0.0, 0.0};
         for (int i = i0; i < C; i += stride) {
-            float ti[3];
-            row_apply<3>(a, i, r, invd, ti);
+            float si[3], ti[3];
 #pragma unroll
             for (int o = 0; o < 3; ++o) {
                 const size_t q = 3 * (size_t)i + o;
+                si[o] = r[q] - af * vn[q];
+                x[q] += af * (pn[q] * invd[q]);
+                ti[o] = diag[q] * (si[o] * invd[q]);
+            }
+            for (int j = 0; j < W; ++j) {
+                const float v = off[(size_t)j * C + i];
+                const int c = col[(size_t)j * C + i];
+#pragma unroll
+                for (int o = 0; o < 3; ++o) {
+                    const size_t q = 3 * (size_t)c + o;
+                    const float sc = r[q] - af * vn[q];
+                    ti[o] += v * (sc * invd[q]);
+                }
+            }
+#pragma unroll
+            for (int o = 0; o < 3; ++o) {
+                const size_t q = 3 * (size_t)i + o;
+                s[q] = si[o];
                 t[q] = ti[o];
                 ts[0] += (double)ti[o] * ti[o];
-                ts[1] += (double)ti[o] * r[q];
+                ts[1] += (double)ti[o] * si[o];
             }
         }
         SYNC(2, ts);
         const double omega = ts[0] != 0.0 ? ts[1] / ts[0] : 0.0;
-        const float of = (float)omega;
+        of = (float)omega;
         // x += omega M s ; r = s - omega t ; r.r ; r0.r
         double rr2[2] = {0.0, 0.0};
         for (int i = i0; i < C; i += stride) {
 #pragma unroll
             for (int o = 0; o < 3; ++o) {
                 const size_t q = 3 * (size_t)i + o;
-                const float si = r[q];
+                const float si = s[q];
                 x[q] += of * (si * invd[q]);
                 const float ri = si - of * t[q];
                 r[q] = ri;
@@ -224,16 +268,8 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
         if (omega == 0.0 || rho == 0.0) { status = WCFD_KRYLOV_BREAKDOWN; break; }
         const double beta = (rr2[1] / rho) * (alpha / omega);
         rho = rr2[1];
-        const float bf = (float)beta;
-        // p = r + beta (p - omega v)
-        for (int i = i0; i < C; i += stride) {
-#pragma unroll
-            for (int o = 0; o < 3; ++o) {
-                const size_t q = 3 * (size_t)i + o;
-                p[q] = r[q] + bf * (p[q] - of * v[q]);
-            }
-        }
-        SYNC(0, nullptr);
+        bf = (float)beta;
+        cur ^= 1;
     }
     write_stats(a, k, rr, status);
 }

@@ -1,0 +1,81 @@
+"""Algorithmic (compulsory) HBM bytes of the kernels of one SIMPLE outer iteration.
+
+Each array a kernel must touch is counted once per launch at its storage width (fp32
+values, int32 indices, float4-packed geometry).  Gathers of neighbour values that a
+kernel already streams elsewhere are not counted again.  C cells, K faces (Ki internal,
+B boundary), F slots per cell, W off-diagonal width, k Krylov iterations.
+"""
+from __future__ import annotations
+
+
+def cg_bytes_per_iteration(C: int, W: int) -> int:
+    """One CG iteration (three phases) per row:
+    q = A p      : off 4W + col 4W + diag 4 + p 4 + q(write) 4
+    x, r update  : x 8 + p 4 + r 8 + q 4 + invd 4
+    p update     : r 4 + invd 4 + p 8
+    """
+    return C * (8 * W + 12 + 28 + 16)
+
+
+def cg_bytes_setup(C: int, W: int) -> int:
+    """r = b - A x, invd, p: off/col 8W, diag 4, x 4, b 4, writes r, invd, p 12."""
+    return C * (8 * W + 24)
+
+
+def cg_bytes(C: int, W: int, iters: int) -> int:
+    return cg_bytes_setup(C, W) + iters * cg_bytes_per_iteration(C, W)
+
+
+def bicgstab_bytes_per_iteration(C: int, W: int) -> int:
+    """One BiCGSTAB iteration on the 3-component system, per cell (12 B per vector):
+    v = A M p : off/col 8W + diag 12 + p 12 + invd 12 + v 12 + r0 12
+    s, x      : r 24 + v 12 + x 24 + p 12 + invd 12
+    t = A M s : off/col 8W + diag 12 + s 12 + invd 12 + t 12
+    x, r      : x 24 + s 12 + invd 12 + t 12 + r 12 + r0 12
+    p         : r 12 + p 24 + v 12
+    """
+    return C * (16 * W + 60 + 84 + 48 + 84 + 48)
+
+
+def bicgstab_bytes(C: int, W: int, iters: int) -> int:
+    setup = C * (8 * W + 12 + 12 + 12 + 12 * 4)
+    return setup + iters * bicgstab_bytes_per_iteration(C, W)
+
+
+def face_pass_bytes(C: int, K: int, Ki: int, B: int, mdot: bool = True) -> int:
+    b = 8 * K + 16 * Ki + 32 * K + 64 * C          # owner/nbr, interp, face values rw, cell values+grads
+    b += B * (4 + 4 + 16 + 32 + 4)                   # brow, bc type, bc value, face grads rw, rpf
+    if mdot:
+        b += 16 * K + 4 * K
+    return b
+
+
+def gradient_bytes(C: int, K: int, F: int, div: bool = False) -> int:
+    b = 16 * F * C + 16 * K + 48 * C
+    if div:
+        b += 4 * K + 4 * C
+    return b
+
+
+def momentum_assembly_bytes(C: int, K: int, F: int, W: int, B: int) -> int:
+    return (16 * F * C + 4 * K + 4 * K + 4 * K + B * (4 + 4 + 16 + 16 + 4) + 4 * W * C + 24 * C + 16 * C + 48 * C
+            + 4 * C + 4 * C)
+
+
+def pressure_assembly_bytes(C: int, K: int, F: int, W: int, B: int) -> int:
+    return 16 * F * C + 4 * K + 4 * K + 4 * K + B * (4 + 1 + 8) + 4 * W * C + 8 * C + 4 * C
+
+
+def simple_step_bytes(C, K, Ki, B, F, W, k_u, k_p, n_corr=1) -> dict:
+    d = {
+        "face_pass": face_pass_bytes(C, K, Ki, B) * 2 * n_corr + face_pass_bytes(C, K, Ki, B, mdot=False) * n_corr,
+        "gradient": gradient_bytes(C, K, F) + gradient_bytes(C, K, F, div=True) * n_corr
+        + gradient_bytes(C, K, F) * n_corr,
+        "momentum_assemble": momentum_assembly_bytes(C, K, F, W, B),
+        "pressure_assemble": pressure_assembly_bytes(C, K, F, W, B) * n_corr,
+        "bicgstab": bicgstab_bytes(C, W, k_u),
+        "cg": cg_bytes(C, W, k_p) * n_corr,
+        "small": 32 * C + 12 * K,
+    }
+    d["total"] = sum(d.values())
+    return d
