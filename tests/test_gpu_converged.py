@@ -46,7 +46,7 @@ def test_converged_cavity_matches_fp64_fixture():
     print(f"converged 64x64 cavity vs fp64 oracle: u {eu:.2e} v {ev:.2e} p {ep:.2e}")
     assert eu < 5e-5 and ev < 5e-5
     assert ep < 2e-3
-    assert np.abs(g[:, 2]).max() == 0.0
+    assert np.abs(g[:, 2]).max() < 1e-6      # 2D case: w stays at rounding level
 
 
 def test_reference_settings_within_oracle_spread():
