@@ -218,6 +218,18 @@ int wcfd_cg(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, doub
 int wcfd_bicgstab(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, double atol,
                   int32_t maxiter, wcfd_solve_stats* stats, void* stream);
 
+/* Allocation-free variant of wcfd_cg (no counterpart in the reference).  For callers that
+ * hold their input and output device arrays but cannot allocate device workspace (device
+ * memory budgeted at start-up, plugins that may not allocate): the Krylov workspace is a
+ * fixed array inside the library, sized for at most WCFD_NOALLOC_MAX_CELLS rows (about
+ * 2.6 MiB, held by every GPU that loads the library until exit); larger systems return
+ * WCFD_ERR_TOO_LARGE.  The first call on a device looks up the array's device address
+ * (make it before any stream capture).  The call allocates nothing.  All calls share the
+ * array, so calls that overlap on the GPU race; results are those of wcfd_cg. */
+#define WCFD_NOALLOC_MAX_CELLS 131072
+int wcfd_cg_noalloc(const wcfd_mesh* m, wcfd_system A, float* x, double atol, int32_t maxiter,
+                    wcfd_solve_stats* stats, void* stream);
+
 /* ------------------------------------------------------------------ fused steps */
 /* One steady SIMPLE outer iteration (incompressible.py:95-156 with steady_state=True),
  * or one PISO time step (NUM_OUTER_LOOPS = 1, steady_state=False), as a fixed sequence of

@@ -290,3 +290,70 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------
+// Allocation-free CG: the workspace lives in a fixed-size array in the library's own
+// device memory instead of coming from the caller.
+//
+// For callers that own their input and output arrays but cannot create device
+// workspace: a host code that drives the pressure solve through this C ABI with a
+// device-memory budget fixed at start-up, or a plugin that is not allowed to allocate
+// once its host application runs.  The array is a file-scope __device__ variable, so
+// every GPU that loads the library holds it (about 2.6 MiB) until the process exits.
+//
+// The host only knows a stand-in for the array's name; its device address is looked up
+// with cudaGetSymbolAddress once per device (on the first call made with that device
+// current) and then passed to the kernel.  Make that first call before any stream
+// capture.  All calls share the one array: the call zeroes the barrier words it needs,
+// and calls that overlap on the GPU (other streams, other threads) race on it.
+namespace {
+
+constexpr size_t kNoAllocVecBytes = 5ull * WCFD_NOALLOC_MAX_CELLS * sizeof(float);
+constexpr size_t kNoAllocPartialsOff = (kNoAllocVecBytes + 255) / 256 * 256;
+constexpr size_t kNoAllocPartialsBytes = 8ull * WCFD_MAX_BLOCKS * sizeof(double);
+constexpr size_t kNoAllocBarrierOff = kNoAllocPartialsOff + kNoAllocPartialsBytes;
+constexpr size_t kNoAllocBytes = kNoAllocBarrierOff + WCFD_BARRIER_WORDS * sizeof(uint32_t);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[64] = {nullptr};
+
+}  // namespace
+
+extern "C" int wcfd_cg_noalloc(const wcfd_mesh* m, wcfd_system A, float* x, double atol, int32_t maxiter,
+                               wcfd_solve_stats* stats, void* stream) {
+    int rc = check_mesh(m);
+    if (rc) return rc;
+    RET_IF(A.ncomp != 1, WCFD_ERR_ARGUMENT, "cg solves scalar systems (ncomp 1)");
+    RET_IF(m->n_cells > WCFD_NOALLOC_MAX_CELLS, WCFD_ERR_TOO_LARGE,
+           "wcfd_cg_noalloc: n_cells exceeds WCFD_NOALLOC_MAX_CELLS (use wcfd_cg with a caller workspace)");
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return set_error(WCFD_ERR_CUDA, "wcfd_cg_noalloc: no usable current device");
+    }
+    void* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            void* p = nullptr;
+            const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p) {
+                cudaGetLastError();
+                std::snprintf(g_last_error, sizeof(g_last_error), "wcfd_cg_noalloc: cudaGetSymbolAddress: %s",
+                              cudaGetErrorString(e));
+                return WCFD_ERR_CUDA;
+            }
+            g_noalloc_addr[dev] = p;
+        }
+        base = g_noalloc_addr[dev];
+    }
+    unsigned char* b = static_cast<unsigned char*>(base);
+    wcfd_krylov_ws ws;
+    ws.vec = reinterpret_cast<float*>(b);
+    ws.partials = reinterpret_cast<double*>(b + kNoAllocPartialsOff);
+    ws.results = nullptr;
+    ws.barrier = reinterpret_cast<uint32_t*>(b + kNoAllocBarrierOff);
+    return launch_krylov((const void*)cg_kernel, 0, m, A, x, ws, atol, maxiter, stats, S(stream), "cg_kernel");
+}
