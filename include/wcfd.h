@@ -215,6 +215,10 @@ int wcfd_spmv(const wcfd_mesh* m, wcfd_system A, const float* x, float* y, void*
  * or maxiter. */
 int wcfd_cg(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, double atol,
             int32_t maxiter, wcfd_solve_stats* stats, void* stream);
+/* Which CG kernel wcfd_cg runs: 0 = automatic (the cluster-resident kernel when the system
+ * fits in the shared memory of one cluster of up to 16 CTAs, else the grid-cooperative
+ * kernel), 1 = always grid-cooperative, 2 = cluster-resident when it fits.  Process-wide. */
+int wcfd_set_krylov_path(int32_t path);
 int wcfd_bicgstab(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, double atol,
                   int32_t maxiter, wcfd_solve_stats* stats, void* stream);
 

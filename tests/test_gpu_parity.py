@@ -187,3 +187,44 @@ def test_runs_are_bitwise_reproducible():
             solver.step()
         outs.append(fields(model))
     assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("case", ["cavity", "channel", "cavity3d"])
+def test_cg_paths_agree_with_oracle(case):
+    """The cluster-resident CG (shared memory of one thread-block cluster) and the
+    grid-cooperative CG solve the same assembled pressure system like the oracle's CG."""
+    import ctypes as ct
+
+    from oracle.simple_ref import cg as oracle_cg, jacobi_inverse
+    from warpcfd_gb300 import _lib
+
+    mk = {"cavity": (lambda: cavity_mesh(40, jitter=0.1, seed=1), cavity_bc, 0),
+          "channel": (lambda: channel_mesh(200, 40), channel_bc, None),
+          "cavity3d": (lambda: cavity3d_mesh(16), cavity3d_bc, 0)}[case]
+    m = mk[0]()
+    model, solver, oc = make_pair(m, mk[1], ref_cell=mk[2])
+    for _ in range(2):
+        solver.step()
+    torch.cuda.synchronize()
+    pe = solver.p_corr_equation
+    A = pe.matrix.to_dense().cpu().numpy().astype(np.float32)
+    import scipy.sparse as sp
+    As = sp.csr_matrix(A)
+    b = pe.rhs.cpu().numpy()
+    xo = np.zeros_like(b)
+    ko, _ = oracle_cg(As, b, xo, jacobi_inverse(np.diag(A).copy()), 1e-6, 300)
+    lib = _lib.load()
+    out = {}
+    try:
+        for path in (1, 2):
+            assert lib.wcfd_set_krylov_path(path) == 0
+            x = torch.zeros_like(pe.x)
+            pe.tol, pe.max_iter = 1e-6, 300
+            st, _ = pe.solve_Axb(x)
+            out[path] = (x.cpu().numpy(), st)
+    finally:
+        lib.wcfd_set_krylov_path(0)
+    for path, (x, st) in out.items():
+        assert abs(st["iterations"] - ko) <= max(2, ko // 50), (path, st, ko)
+        assert rel_l2(x, xo) < 1e-4, path
+    assert rel_l2(out[1][0], out[2][0]) < 1e-4

@@ -51,8 +51,14 @@ def test_noalloc_cg_matches_workspace_cg():
 
     x_ref = torch.zeros(C, dtype=torch.float32, device="cuda")
     st_ref = torch.zeros(16, dtype=torch.uint8, device="cuda")
-    rc = lib.wcfd_cg(ct.byref(mesh_t), pe.system_struct(), ct.c_void_p(x_ref.data_ptr()), pe.workspace_struct(),
-                     1e-6, 500, ct.c_void_p(st_ref.data_ptr()), stream)
+    # the reference result comes from wcfd_cg on its grid-cooperative kernel, the one the
+    # allocation-free entry point runs, so the two must agree to the last bit
+    assert lib.wcfd_set_krylov_path(1) == 0
+    try:
+        rc = lib.wcfd_cg(ct.byref(mesh_t), pe.system_struct(), ct.c_void_p(x_ref.data_ptr()),
+                         pe.workspace_struct(), 1e-6, 500, ct.c_void_p(st_ref.data_ptr()), stream)
+    finally:
+        lib.wcfd_set_krylov_path(0)
     assert rc == 0, lib.wcfd_last_error()
     torch.cuda.synchronize()
     it_ref, status_ref, _ = _stats(st_ref)

@@ -91,6 +91,7 @@ _SIGS = {
     "wcfd_cg": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, KrylovWS_t, ct.c_double, ct.c_int32, vp, vp]),
     "wcfd_bicgstab": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, KrylovWS_t, ct.c_double, ct.c_int32, vp, vp]),
     "wcfd_simple_iteration": (ct.c_int, [ct.POINTER(Case_t), vp]),
+    "wcfd_set_krylov_path": (ct.c_int, [ct.c_int32]),
 }
 
 EXPORTED = tuple(_SIGS.keys())

@@ -51,25 +51,24 @@ int check_mesh(const wcfd_mesh* m) {
 
 inline cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
-// co-resident blocks of a cooperative kernel on the current device (cached per device)
-int coop_capacity(const void* fn, int slot) {
+// co-resident blocks of a cooperative kernel on the current device (cached per kernel
+// and device)
+int coop_capacity(const void* fn, int /*unused*/) {
     static std::mutex mu;
-    static int cache[2][64];
-    static bool init = false;
+    struct Entry { const void* fn; int dev; int cap; };
+    static Entry cache[64];
+    static int n = 0;
     int dev = 0;
     cudaGetDevice(&dev);
     std::lock_guard<std::mutex> lk(mu);
-    if (!init) {
-        std::memset(cache, 0, sizeof(cache));
-        init = true;
-    }
-    if (dev < 64 && cache[slot][dev] > 0) return cache[slot][dev];
+    for (int i = 0; i < n; ++i)
+        if (cache[i].fn == fn && cache[i].dev == dev) return cache[i].cap;
     int per_sm = 0, sms = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kSolverBlock, 0);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int cap = per_sm * sms;
     if (cap > WCFD_MAX_BLOCKS) cap = WCFD_MAX_BLOCKS;
-    if (dev < 64) cache[slot][dev] = cap;
+    if (n < 64) cache[n++] = Entry{fn, dev, cap};
     return cap;
 }
 
@@ -77,6 +76,7 @@ int launch_krylov(const void* fn, int slot, const wcfd_mesh* m, wcfd_system A, f
                   double atol, int maxiter, wcfd_solve_stats* stats, cudaStream_t st, const char* name) {
     int rc = check_mesh(m);
     if (rc) return rc;
+    RET_IF(!fn, WCFD_ERR_ARGUMENT, "no solver kernel for this off-diagonal width");
     RET_IF(!A.diag || !A.off || !A.rhs || !x || !ws.vec || !ws.partials || !ws.barrier || !stats,
            WCFD_ERR_ARGUMENT, "null solver argument");
     RET_IF(maxiter < 0 || !(atol >= 0.0), WCFD_ERR_ARGUMENT, "bad atol or maxiter");
@@ -109,11 +109,94 @@ int launch_krylov(const void* fn, int slot, const wcfd_mesh* m, wcfd_system A, f
     return WCFD_OK;
 }
 
+int g_krylov_path = 0;  // 0 automatic, 1 grid-cooperative only, 2 cluster-resident when it fits
+
+// Cluster-resident CG when the system fits in the shared memory of one cluster of up to
+// 16 CTAs; returns -1 (caller falls back to the grid-cooperative kernel) otherwise.
+int try_cluster_cg(const wcfd_mesh* m, wcfd_system A, float* x, double atol, int maxiter,
+                   wcfd_solve_stats* stats, cudaStream_t st) {
+    if (g_krylov_path == 1) return -1;
+    const int C = m->n_cells, W = m->ell_width;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const long long budget = (long long)optin - 8192;  // static shared memory and reserve
+    if (budget <= 0) return -1;
+    const long long rmax = budget / (8LL * W + 28);
+    int cs = 0, R = 0;
+    for (int c = 1; c <= 16; c *= 2) {
+        const long long r = (C + c - 1) / c;
+        if (r <= rmax && (r <= 2048 || c == 16)) {
+            cs = c;
+            R = (int)r;
+            break;
+        }
+    }
+    if (cs == 0) return -1;
+    const size_t smem = cluster_cg_smem_bytes(R, W);
+    const void* fn = cg_cluster_kernel_for(W);
+    if (!fn) return -1;
+    static std::mutex mu;
+    static size_t set_bytes[64][7] = {{0}};
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (dev >= 64) return -1;
+        if (set_bytes[dev][W] < smem) {
+            if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+                cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+                cudaGetLastError();
+                return -1;
+            }
+            set_bytes[dev][W] = smem;
+        }
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cs);
+    cfg.blockDim = dim3(kClusterBlock);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, fn, &cfg) != cudaSuccess ||
+        nclusters < 1) {
+        cudaGetLastError();
+        return -1;
+    }
+    KrylovArgs a = {};
+    a.m = *m;
+    a.A = A;
+    a.x = x;
+    a.atol2 = atol * atol;
+    a.maxiter = maxiter;
+    a.stats = stats;
+    void* args[] = {&a, &R};
+    const cudaError_t e = cudaLaunchKernelExC(&cfg, fn, args);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        std::snprintf(g_last_error, sizeof(g_last_error), "cg_cluster_kernel: %s", cudaGetErrorString(e));
+        return WCFD_ERR_CUDA;
+    }
+    return WCFD_OK;
+}
+
 }  // namespace
 
 extern "C" {
 
 int wcfd_version(void) { return 100; }
+
+int wcfd_set_krylov_path(int32_t path) {
+    if (path < 0 || path > 2) return set_error(WCFD_ERR_ARGUMENT, "path must be 0 (auto), 1 (grid), 2 (cluster)");
+    g_krylov_path = path;
+    return WCFD_OK;
+}
 
 const char* wcfd_last_error(void) { return g_last_error; }
 
@@ -219,13 +302,19 @@ int wcfd_spmv(const wcfd_mesh* m, wcfd_system A, const float* x, float* y, void*
 int wcfd_cg(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, double atol, int32_t maxiter,
             wcfd_solve_stats* stats, void* stream) {
     RET_IF(A.ncomp != 1, WCFD_ERR_ARGUMENT, "cg solves scalar systems (ncomp 1)");
-    return launch_krylov((const void*)cg_kernel, 0, m, A, x, ws, atol, maxiter, stats, S(stream), "cg_kernel");
+    int rc = check_mesh(m);
+    if (rc) return rc;
+    RET_IF(!A.diag || !A.off || !A.rhs || !x || !stats, WCFD_ERR_ARGUMENT, "null solver argument");
+    RET_IF(maxiter < 0 || !(atol >= 0.0), WCFD_ERR_ARGUMENT, "bad atol or maxiter");
+    rc = try_cluster_cg(m, A, x, atol, maxiter, stats, S(stream));
+    if (rc >= 0) return rc;
+    return launch_krylov(cg_kernel_for(m->ell_width), 0, m, A, x, ws, atol, maxiter, stats, S(stream), "cg_kernel");
 }
 
 int wcfd_bicgstab(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, double atol, int32_t maxiter,
                   wcfd_solve_stats* stats, void* stream) {
     RET_IF(A.ncomp != 3, WCFD_ERR_ARGUMENT, "bicgstab solves the 3-component momentum system (ncomp 3)");
-    return launch_krylov((const void*)bicgstab_kernel, 1, m, A, x, ws, atol, maxiter, stats, S(stream),
+    return launch_krylov(bicgstab_kernel_for(m->ell_width), 1, m, A, x, ws, atol, maxiter, stats, S(stream),
                          "bicgstab_kernel");
 }
 
@@ -355,5 +444,5 @@ extern "C" int wcfd_cg_noalloc(const wcfd_mesh* m, wcfd_system A, float* x, doub
     ws.partials = reinterpret_cast<double*>(b + kNoAllocPartialsOff);
     ws.results = nullptr;
     ws.barrier = reinterpret_cast<uint32_t*>(b + kNoAllocBarrierOff);
-    return launch_krylov((const void*)cg_kernel, 0, m, A, x, ws, atol, maxiter, stats, S(stream), "cg_kernel");
+    return launch_krylov(cg_kernel_for(m->ell_width), 0, m, A, x, ws, atol, maxiter, stats, S(stream), "cg_kernel");
 }

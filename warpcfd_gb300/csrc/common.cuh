@@ -12,6 +12,7 @@ namespace wcfd {
 constexpr int kBlock = 256;      // threads of the one-thread-per-face/cell kernels
 constexpr int kSolverBlock = 512;  // threads of the persistent Krylov kernels
 constexpr int kMaxSlots = 6;     // faces per cell (hex)
+constexpr int kClusterBlock = 1024;  // threads per CTA of the cluster-resident solver
 
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }

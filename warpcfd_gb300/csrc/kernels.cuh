@@ -37,8 +37,11 @@ struct KrylovArgs {
     int maxiter;
     wcfd_solve_stats* stats;
 };
-__global__ void cg_kernel(KrylovArgs a);
-__global__ void bicgstab_kernel(KrylovArgs a);
+// kernel instantiations for off-diagonal width W (0..6), nullptr otherwise
+const void* cg_kernel_for(int W);
+const void* bicgstab_kernel_for(int W);
+const void* cg_cluster_kernel_for(int W);
+size_t cluster_cg_smem_bytes(int R, int W);
 
 inline int grid_for(long long n, int bs = kBlock) { return (int)((n + bs - 1) / bs); }
 

@@ -47,11 +47,12 @@ __device__ void write_stats(const KrylovArgs& a, int k, double rr, int status) {
     }
 }
 
-// Jacobi-preconditioned CG on a scalar system.
+// Jacobi-preconditioned CG on a scalar system, W = off-diagonal width known at compile
+// time so the loads of a row's columns and gathered values are all in flight at once.
 // Workspace: r, pA, pB, q, invd (5 C floats).
+template <int W>
 __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
     const int C = a.m.n_cells;
-    const int W = a.m.ell_width;
     float* r = a.ws;
     float* pbuf[2] = {a.ws + (size_t)C, a.ws + 2 * (size_t)C};
     float* q = a.ws + 3 * (size_t)C;
@@ -70,6 +71,7 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
     double red[2] = {0.0, 0.0};
     for (int i = i0; i < C; i += stride) {
         float ax = diag[i] * x[i];
+#pragma unroll
         for (int j = 0; j < W; ++j) ax += off[(size_t)j * C + i] * x[col[(size_t)j * C + i]];
         const float ri = b[i] - ax;
         const float di = jacobi(diag[i]);
@@ -92,7 +94,9 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
         for (int i = i0; i < C; i += stride) {
             const float pi = r[i] * invd[i] + bf * po[i];
             float qi = diag[i] * pi;
-            for (int j = 0; j < W; ++j) {
+#pragma unroll
+    #pragma unroll
+        for (int j = 0; j < W; ++j) {
                 const int c = col[(size_t)j * C + i];
                 qi += off[(size_t)j * C + i] * (r[c] * invd[c] + bf * po[c]);
             }
@@ -128,9 +132,9 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
 // Right-preconditioned (Jacobi) BiCGSTAB on the 3-component momentum system
 // (interleaved rows 3c+o, shared off-diagonals).
 // Workspace (3C floats each): r, r0, pA, pB, vA, vB, t, s, invd.
+template <int W>
 __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
     const int C = a.m.n_cells;
-    const int W = a.m.ell_width;
     const size_t n3 = 3 * (size_t)C;
     float* r = a.ws;
     float* r0 = a.ws + n3;
@@ -155,6 +159,7 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
         float ax[3];
 #pragma unroll
         for (int o = 0; o < 3; ++o) ax[o] = diag[3 * (size_t)i + o] * x[3 * (size_t)i + o];
+#pragma unroll
         for (int j = 0; j < W; ++j) {
             const float v = off[(size_t)j * C + i];
             const int c = col[(size_t)j * C + i];
@@ -193,7 +198,9 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
                 pi[o] = r[q] + bf * (po[q] - of * vo[q]);
                 vi[o] = diag[q] * (pi[o] * invd[q]);
             }
-            for (int j = 0; j < W; ++j) {
+#pragma unroll
+    #pragma unroll
+        for (int j = 0; j < W; ++j) {
                 const float v = off[(size_t)j * C + i];
                 const int c = col[(size_t)j * C + i];
 #pragma unroll
@@ -226,7 +233,9 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
                 x[q] += af * (pn[q] * invd[q]);
                 ti[o] = diag[q] * (si[o] * invd[q]);
             }
-            for (int j = 0; j < W; ++j) {
+#pragma unroll
+    #pragma unroll
+        for (int j = 0; j < W; ++j) {
                 const float v = off[(size_t)j * C + i];
                 const int c = col[(size_t)j * C + i];
 #pragma unroll
@@ -272,6 +281,32 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
         cur ^= 1;
     }
     write_stats(a, k, rr, status);
+}
+
+const void* cg_kernel_for(int W) {
+    switch (W) {
+        case 0: return (const void*)cg_kernel<0>;
+        case 1: return (const void*)cg_kernel<1>;
+        case 2: return (const void*)cg_kernel<2>;
+        case 3: return (const void*)cg_kernel<3>;
+        case 4: return (const void*)cg_kernel<4>;
+        case 5: return (const void*)cg_kernel<5>;
+        case 6: return (const void*)cg_kernel<6>;
+        default: return nullptr;
+    }
+}
+
+const void* bicgstab_kernel_for(int W) {
+    switch (W) {
+        case 0: return (const void*)bicgstab_kernel<0>;
+        case 1: return (const void*)bicgstab_kernel<1>;
+        case 2: return (const void*)bicgstab_kernel<2>;
+        case 3: return (const void*)bicgstab_kernel<3>;
+        case 4: return (const void*)bicgstab_kernel<4>;
+        case 5: return (const void*)bicgstab_kernel<5>;
+        case 6: return (const void*)bicgstab_kernel<6>;
+        default: return nullptr;
+    }
 }
 
 }  // namespace wcfd

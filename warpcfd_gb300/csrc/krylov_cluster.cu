@@ -1,0 +1,202 @@
+// Cluster-resident CG: one thread-block cluster (up to 16 CTAs) holds the whole scalar
+// system in shared memory for the length of the solve.
+//
+//  * CTA q of the cluster owns rows [q R, (q+1) R); its slice of the matrix (off-diagonals,
+//    packed (rank, local) columns, diagonal) and of every vector lives in its shared memory.
+//  * A neighbour value owned by another CTA is read through distributed shared memory
+//    (mapa + ld.shared::cluster); nothing touches global memory between the set-up and
+//    the final write of x.
+//  * Grid-wide synchronisation is the hardware cluster barrier
+//    (barrier.cluster.arrive.release / wait.acquire).  A dot product is an all-reduce: each
+//    CTA sums its rows, stores the block total into a slot of every CTA's shared memory,
+//    and after the barrier every CTA adds the CS slots in rank order, so all CTAs (and all
+//    runs) agree bit for bit.  All CTAs take the same branch at every test, so no CTA can
+//    leave while another still waits or reads its memory.
+//  * The direction update p = z + beta p is evaluated inside the SpMV for the row and its
+//    neighbours (double-buffered p), so an iteration needs two barriers.
+// The arithmetic is that of cg_kernel (krylov.cu): the same Jacobi-preconditioned CG with
+// fp64 dot products and the same stop test.
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace wcfd {
+
+constexpr int CBS = kClusterBlock;
+
+__device__ __forceinline__ unsigned cluster_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned cluster_nranks() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// shared::cluster address of `p` (a pointer into this CTA's shared memory) in CTA `rank`
+__device__ __forceinline__ uint32_t map_rank(const void* p, unsigned rank) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ float ld_cluster_f32(uint32_t addr) {
+    float v;
+    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(addr) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_cluster_f64(uint32_t addr, double v) {
+    asm volatile("st.shared::cluster.f64 [%0], %1;" :: "r"(addr), "d"(v) : "memory");
+}
+
+// all-reduce of NV doubles over the cluster; slots double-buffered by `parity`
+template <int NV>
+__device__ __forceinline__ void cluster_allreduce(double (&v)[NV], double* slots, unsigned parity, unsigned me,
+                                                  unsigned cs) {
+    block_sum<NV, CBS>(v);
+    double* base = slots + parity * (NV * 16);
+    if (threadIdx.x < cs) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) st_cluster_f64(map_rank(base + i * 16 + me, threadIdx.x), v[i]);
+    }
+    cluster_sync_all();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        double s = 0.0;
+        for (unsigned q = 0; q < cs; ++q) s += base[i * 16 + q];
+        v[i] = s;
+    }
+}
+
+// dynamic shared memory per CTA for R rows and width W:
+// off + packed columns (8 W) and diag, invd, x, r, p (two buffers), q (28)
+size_t cluster_cg_smem_bytes(int R, int W) { return (size_t)R * (8 * (size_t)W + 28); }
+
+template <int W>
+__global__ void __launch_bounds__(CBS) cg_cluster_kernel(KrylovArgs a, int R) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double slots[2 * 2 * 16];
+    const int C = a.m.n_cells;
+    const unsigned me = cluster_rank();
+    const unsigned cs = cluster_nranks();
+    const int row0 = (int)me * R;
+    const int nloc = max(0, min(R, C - row0));
+    float* off = reinterpret_cast<float*>(smem);                 // [W][R]
+    uint32_t* colp = reinterpret_cast<uint32_t*>(off + (size_t)W * R);  // [W][R] (rank << 24) | local
+    float* diag = reinterpret_cast<float*>(colp + (size_t)W * R);
+    float* invd = diag + R;
+    float* x = invd + R;
+    float* r = x + R;
+    float* pbuf0 = r + R;
+    float* pbuf1 = pbuf0 + R;
+    float* q = pbuf1 + R;
+    int k = 0, status = WCFD_OK;
+
+    // load this CTA's slice
+    for (int l = threadIdx.x; l < nloc; l += CBS) {
+        const int g = row0 + l;
+        diag[l] = a.A.diag[g];
+        invd[l] = diag[l] != 0.0f ? 1.0f / diag[l] : 1.0f;
+        x[l] = a.x[g];
+#pragma unroll
+        for (int j = 0; j < W; ++j) {
+            off[(size_t)j * R + l] = a.A.off[(size_t)j * C + g];
+            const int c = a.m.ell_col[(size_t)j * C + g];
+            const int rk = c / R;
+            colp[(size_t)j * R + l] = ((uint32_t)rk << 24) | (uint32_t)(c - rk * R);
+        }
+    }
+    cluster_sync_all();
+    // r = b - A x ; p = z = M r ; rr ; rz
+    double red[2] = {0.0, 0.0};
+    for (int l = threadIdx.x; l < nloc; l += CBS) {
+        float ax = diag[l] * x[l];
+#pragma unroll
+        for (int j = 0; j < W; ++j) {
+            const uint32_t cp = colp[(size_t)j * R + l];
+            ax += off[(size_t)j * R + l] * ld_cluster_f32(map_rank(x + (cp & 0xFFFFFFu), cp >> 24));
+        }
+        const float ri = a.A.rhs[row0 + l] - ax;
+        const float zi = ri * invd[l];
+        r[l] = ri;
+        pbuf0[l] = zi;
+        red[0] += (double)ri * ri;
+        red[1] += (double)ri * zi;
+    }
+    unsigned parity = 0;
+    cluster_allreduce<2>(red, slots, parity, me, cs);
+    parity ^= 1u;
+    double rr = red[0], rz = red[1];
+    float bf = 0.0f;
+    int cur = 0;
+    while (k < a.maxiter && rr > a.atol2) {
+        float* po = cur ? pbuf1 : pbuf0;
+        float* pn = cur ? pbuf0 : pbuf1;
+        double pq[1] = {0.0};
+        for (int l = threadIdx.x; l < nloc; l += CBS) {
+            const float pi = r[l] * invd[l] + bf * po[l];
+            float qi = diag[l] * pi;
+    #pragma unroll
+        for (int j = 0; j < W; ++j) {
+                const uint32_t cp = colp[(size_t)j * R + l];
+                const unsigned rk = cp >> 24;
+                const uint32_t lo = cp & 0xFFFFFFu;
+                const float rc = ld_cluster_f32(map_rank(r + lo, rk));
+                const float dc = ld_cluster_f32(map_rank(invd + lo, rk));
+                const float pc = ld_cluster_f32(map_rank(po + lo, rk));
+                qi += off[(size_t)j * R + l] * (rc * dc + bf * pc);
+            }
+            pn[l] = pi;
+            q[l] = qi;
+            pq[0] += (double)pi * qi;
+        }
+        cluster_allreduce<1>(pq, slots, parity, me, cs);
+        parity ^= 1u;
+        if (pq[0] == 0.0) { status = WCFD_KRYLOV_BREAKDOWN; break; }
+        const double alpha = rz / pq[0];
+        const float af = (float)alpha;
+        double red2[2] = {0.0, 0.0};
+        for (int l = threadIdx.x; l < nloc; l += CBS) {
+            x[l] += af * pn[l];
+            const float ri = r[l] - af * q[l];
+            r[l] = ri;
+            const float zi = ri * invd[l];
+            red2[0] += (double)ri * ri;
+            red2[1] += (double)ri * zi;
+        }
+        cluster_allreduce<2>(red2, slots, parity, me, cs);
+        parity ^= 1u;
+        rr = red2[0];
+        const double beta = rz != 0.0 ? red2[1] / rz : 0.0;
+        rz = red2[1];
+        bf = (float)beta;
+        cur ^= 1;
+        ++k;
+    }
+    for (int l = threadIdx.x; l < nloc; l += CBS) a.x[row0 + l] = x[l];
+    if (me == 0 && threadIdx.x == 0) {
+        int st = status;
+        if (st == WCFD_OK && !(rr <= a.atol2)) st = WCFD_NOT_CONVERGED;
+        a.stats->iterations = k;
+        a.stats->status = st;
+        a.stats->residual = sqrt(rr);
+    }
+}
+
+const void* cg_cluster_kernel_for(int W) {
+    switch (W) {
+        case 0: return (const void*)cg_cluster_kernel<0>;
+        case 1: return (const void*)cg_cluster_kernel<1>;
+        case 2: return (const void*)cg_cluster_kernel<2>;
+        case 3: return (const void*)cg_cluster_kernel<3>;
+        case 4: return (const void*)cg_cluster_kernel<4>;
+        case 5: return (const void*)cg_cluster_kernel<5>;
+        case 6: return (const void*)cg_cluster_kernel<6>;
+        default: return nullptr;
+    }
+}
+
+}  // namespace wcfd
