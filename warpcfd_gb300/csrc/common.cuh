@@ -41,32 +41,79 @@ __device__ __forceinline__ uint64_t global_ns() {
 // WCFD_BARRIER_TIMEOUT (a healthy wait is one solver phase: microseconds).
 constexpr uint64_t kBarrierTimeoutNs = 1500ull * 1000ull * 1000ull;
 
-// Sum NV doubles over the block; the result is valid in every thread.
+// ---------------------------------------------------------------------------------
+// fp64-accurate dot products without per-element fp64 arithmetic.
+//
+// GB300 executes fp64 at about 1/64 of its fp32 rate, so a cast and an fp64 FMA per
+// element would dominate a bandwidth-bound Krylov phase.  Instead each product is formed
+// exactly as an unevaluated sum h + r (TwoProduct with an FMA) and accumulated in
+// float-float arithmetic (Knuth's TwoSum), the "Dot2" scheme of Ogita, Rump and Oishi,
+// "Accurate sum and dot product", SIAM J. Sci. Comput. 26 (2005): the result is as accurate
+// as if it were computed in twice the working precision.  Per-warp totals are converted to
+// fp64 and every sum across warps, blocks and CTAs is done in fp64 in a fixed order.
+// __fmul_rn / __fadd_rn keep the compiler from contracting the error-free transforms.
+struct ff {
+    float hi, lo;
+};
+
+__device__ __forceinline__ ff ff_zero() { return ff{0.0f, 0.0f}; }
+
+// acc += a * b
+__device__ __forceinline__ void ff_fma(ff& acc, float a, float b) {
+    const float h = __fmul_rn(a, b);
+    const float r = fmaf(a, b, -h);
+    const float s = __fadd_rn(acc.hi, h);
+    const float bb = __fsub_rn(s, acc.hi);
+    const float q = __fadd_rn(__fsub_rn(acc.hi, __fsub_rn(s, bb)), __fsub_rn(h, bb));
+    acc.hi = s;
+    acc.lo = __fadd_rn(acc.lo, __fadd_rn(q, r));
+}
+
+// a += b (symmetric: merging a into b gives the same bits, so butterfly shuffles agree)
+__device__ __forceinline__ void ff_merge(ff& a, const ff& b) {
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    const float q = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    a.hi = s;
+    a.lo = __fadd_rn(__fadd_rn(a.lo, b.lo), q);
+}
+
+// Block total of NV float-float accumulators as fp64, valid in every thread.
 template <int NV, int BS>
-__device__ __forceinline__ void block_sum(double (&v)[NV]) {
-    __shared__ double red[NV][BS / 32];
+__device__ __forceinline__ void block_reduce_ff(ff (&v)[NV], double (&out)[NV]) {
+    __shared__ double wsum[NV][BS / 32];
+    __shared__ double res[NV];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
-        double x = v[i];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-        if (lane == 0) red[i][wid] = x;
+        for (int o = 16; o > 0; o >>= 1) {
+            ff t;
+            t.hi = __shfl_xor_sync(0xffffffffu, v[i].hi, o);
+            t.lo = __shfl_xor_sync(0xffffffffu, v[i].lo, o);
+            ff_merge(v[i], t);
+        }
+        if (lane == 0) wsum[i][wid] = (double)v[i].hi + (double)v[i].lo;
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double x = lane < BS / 32 ? wsum[i][lane] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane == 0) res[i] = x;
+        }
     }
     __syncthreads();
 #pragma unroll
-    for (int i = 0; i < NV; ++i) {
-        double x = lane < BS / 32 ? red[i][lane] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-        v[i] = x;
-    }
+    for (int i = 0; i < NV; ++i) out[i] = res[i];
     __syncthreads();
 }
 
 // Grid-wide synchronisation state living in caller-provided global memory.
 //   flags[b]   phase number block b has reached (zeroed before each launch)
-//   partials   [2 phase parities][4 values][WCFD_MAX_BLOCKS] per-block partial sums
+//   partials   [2 phase parities][4 values][WCFD_MAX_BLOCKS] per-block totals
 struct GridCtl {
     double* partials;
     unsigned* flags;
@@ -74,32 +121,27 @@ struct GridCtl {
 };
 
 // Barrier + reduction over all blocks of a cooperative launch, for phase number `phase`
-// (1, 2, 3, ... in every block).  Each block publishes its NV partial sums and then its
-// flag with one release store (no atomics); every block waits for all flags (one thread
-// per flag, in parallel) and sums the partials in block-index order, so every block gets
-// the same bits on every run.  Partials are double-buffered by phase parity: a block can
-// only overwrite a buffer after every block has passed the phase that read it.
-// Every wait is bounded: on timeout the block sets *err and returns false.
+// (1, 2, 3, ... in every block).  v[] holds this block's fp64 totals (from
+// block_reduce_ff) and returns the grid-wide sums.  Each block publishes its totals and
+// then its flag with one release store (no atomics); all threads of every block wait for
+// the flags in parallel, then warp 0 adds the totals in block-index order, so every block
+// gets the same bits on every run.  Totals are double-buffered by phase parity: a block can
+// only overwrite a buffer after every block has passed the phase that read it.  Every wait
+// is bounded: on timeout the block sets *err and returns false.
 template <int NV, int BS>
 __device__ bool grid_sync(const GridCtl& g, double* v, unsigned phase) {
     __shared__ int s_fail;
+    __shared__ double s_res[NV > 0 ? NV : 1];
     if (threadIdx.x == 0) s_fail = 0;
+    double* pb = g.partials + (size_t)(phase & 1u) * 4 * WCFD_MAX_BLOCKS;
     if constexpr (NV > 0) {
-        double t[NV];
-#pragma unroll
-        for (int i = 0; i < NV; ++i) t[i] = v[i];
-        block_sum<NV, BS>(t);
         if (threadIdx.x == 0) {
-            double* pb = g.partials + (size_t)(phase & 1u) * 4 * WCFD_MAX_BLOCKS;
 #pragma unroll
-            for (int i = 0; i < NV; ++i) pb[i * WCFD_MAX_BLOCKS + blockIdx.x] = t[i];
+            for (int i = 0; i < NV; ++i) pb[i * WCFD_MAX_BLOCKS + blockIdx.x] = v[i];
         }
     }
     __syncthreads();  // this block's writes of the phase happen before its release
     if (threadIdx.x == 0) st_release(g.flags + blockIdx.x, phase);
-    double acc[NV > 0 ? NV : 1];
-#pragma unroll
-    for (int i = 0; i < (NV > 0 ? NV : 1); ++i) acc[i] = 0.0;
     bool ok = true;
     for (int j = threadIdx.x; j < (int)gridDim.x; j += BS) {
         if ((int)(ld_acquire(g.flags + j) - phase) < 0) {
@@ -110,28 +152,35 @@ __device__ bool grid_sync(const GridCtl& g, double* v, unsigned phase) {
                     ok = false;
                     break;
                 }
-                __nanosleep(20);
+                __nanosleep(32);
             }
         }
         if (!ok) break;
-        if constexpr (NV > 0) {
-            const double* pb = g.partials + (size_t)(phase & 1u) * 4 * WCFD_MAX_BLOCKS;
-#pragma unroll
-            for (int i = 0; i < NV; ++i) acc[i] += __ldcg(pb + i * WCFD_MAX_BLOCKS + j);
-        }
     }
     if (!ok) {
         atomicExch(g.err, WCFD_BARRIER_TIMEOUT);
         s_fail = 1;
     }
+    __syncthreads();
+    if (s_fail) return false;
     if constexpr (NV > 0) {
-        block_sum<NV, BS>(acc);  // contains __syncthreads, so s_fail is visible after it
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x;
 #pragma unroll
-        for (int i = 0; i < NV; ++i) v[i] = acc[i];
-    } else {
+            for (int i = 0; i < NV; ++i) {
+                double x = 0.0;
+                for (int j = lane; j < (int)gridDim.x; j += 32) x += __ldcg(pb + i * WCFD_MAX_BLOCKS + j);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+                if (lane == 0) s_res[i] = x;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < NV; ++i) v[i] = s_res[i];
         __syncthreads();
     }
-    return s_fail == 0;
+    return true;
 }
 
 }  // namespace wcfd

@@ -1,6 +1,7 @@
 // Persistent Krylov solvers: one cooperative launch per solve, rows distributed
-// grid-stride over all co-resident blocks, fp64 dot products reduced deterministically
-// at bounded grid barriers (common.cuh).  They replace warp.optim.linear.cg / bicgstab
+// grid-stride over all co-resident blocks, fp64-accurate dot products (exact products
+// summed in float-float within a warp, fp64 across warps and blocks; common.cuh) reduced
+// deterministically at bounded grid barriers.  They replace warp.optim.linear.cg / bicgstab
 // with the diagonal (Jacobi) preconditioner as called by Equation.solve_Axb
 // (warp_cfd/FV/terms/equation.py:195-200).  Stop test: ||r||_2 <= atol before an
 // iteration, or maxiter iterations.
@@ -68,7 +69,7 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
     int k = 0, status = WCFD_OK;
 
     // r = b - A x ; z = M r ; p = z ; rr = r.r ; rz = r.z
-    double red[2] = {0.0, 0.0};
+    ff acc[2] = {ff_zero(), ff_zero()};
     for (int i = i0; i < C; i += stride) {
         float ax = diag[i] * x[i];
 #pragma unroll
@@ -79,9 +80,11 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
         r[i] = ri;
         invd[i] = di;
         pbuf[0][i] = zi;
-        red[0] += (double)ri * ri;
-        red[1] += (double)ri * zi;
+        ff_fma(acc[0], ri, ri);
+        ff_fma(acc[1], ri, zi);
     }
+    double red[2];
+    block_reduce_ff<2, BS>(acc, red);
     SYNC(2, red);
     double rr = red[0], rz = red[1];
     float bf = 0.0f;  // first direction is z itself
@@ -90,34 +93,37 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
         const float* po = pbuf[cur];  // written by other blocks in this launch: no restrict
         float* pn = pbuf[cur ^ 1];
         // p_new = z + beta p_old (here and for every neighbour) ; q = A p_new ; p.q
-        double pq[1] = {0.0};
+        ff accq[1] = {ff_zero()};
         for (int i = i0; i < C; i += stride) {
             const float pi = r[i] * invd[i] + bf * po[i];
             float qi = diag[i] * pi;
 #pragma unroll
-    #pragma unroll
-        for (int j = 0; j < W; ++j) {
+            for (int j = 0; j < W; ++j) {
                 const int c = col[(size_t)j * C + i];
                 qi += off[(size_t)j * C + i] * (r[c] * invd[c] + bf * po[c]);
             }
             pn[i] = pi;
             q[i] = qi;
-            pq[0] += (double)pi * qi;
+            ff_fma(accq[0], pi, qi);
         }
+        double pq[1];
+        block_reduce_ff<1, BS>(accq, pq);
         SYNC(1, pq);
         if (pq[0] == 0.0) { status = WCFD_KRYLOV_BREAKDOWN; break; }
         const double alpha = rz / pq[0];
         const float af = (float)alpha;
         // x += alpha p ; r -= alpha q ; rr ; rz
-        double red2[2] = {0.0, 0.0};
+        ff acc2[2] = {ff_zero(), ff_zero()};
         for (int i = i0; i < C; i += stride) {
             x[i] += af * pn[i];
             const float ri = r[i] - af * q[i];
             r[i] = ri;
             const float zi = ri * invd[i];
-            red2[0] += (double)ri * ri;
-            red2[1] += (double)ri * zi;
+            ff_fma(acc2[0], ri, ri);
+            ff_fma(acc2[1], ri, zi);
         }
+        double red2[2];
+        block_reduce_ff<2, BS>(acc2, red2);
         SYNC(2, red2);
         rr = red2[0];
         const double beta = rz != 0.0 ? red2[1] / rz : 0.0;
@@ -154,7 +160,7 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
     int k = 0, status = WCFD_OK;
 
     // r = b - A x ; r0 = r ; p = r ; v = 0 ; rr ; rho = r0.r = rr
-    double red[1] = {0.0};
+    ff acc[1] = {ff_zero()};
     for (int i = i0; i < C; i += stride) {
         float ax[3];
 #pragma unroll
@@ -175,9 +181,11 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
             pbuf[0][q] = ri;
             vbuf[0][q] = 0.0f;
             invd[q] = jacobi(diag[q]);
-            red[0] += (double)ri * ri;
+            ff_fma(acc[0], ri, ri);
         }
     }
+    double red[1];
+    block_reduce_ff<1, BS>(acc, red);
     SYNC(1, red);
     double rr = red[0];
     double rho = rr;
@@ -189,7 +197,7 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
         float* pn = pbuf[cur ^ 1];
         float* vn = vbuf[cur ^ 1];
         // p = r + beta (p - omega v) ; v = A (M p) ; r0.v
-        double r0v[1] = {0.0};
+        ff accv[1] = {ff_zero()};
         for (int i = i0; i < C; i += stride) {
             float pi[3], vi[3];
 #pragma unroll
@@ -199,8 +207,7 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
                 vi[o] = diag[q] * (pi[o] * invd[q]);
             }
 #pragma unroll
-    #pragma unroll
-        for (int j = 0; j < W; ++j) {
+            for (int j = 0; j < W; ++j) {
                 const float v = off[(size_t)j * C + i];
                 const int c = col[(size_t)j * C + i];
 #pragma unroll
@@ -215,15 +222,17 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
                 const size_t q = 3 * (size_t)i + o;
                 pn[q] = pi[o];
                 vn[q] = vi[o];
-                r0v[0] += (double)r0[q] * vi[o];
+                ff_fma(accv[0], r0[q], vi[o]);
             }
         }
+        double r0v[1];
+        block_reduce_ff<1, BS>(accv, r0v);
         SYNC(1, r0v);
         if (r0v[0] == 0.0) { status = WCFD_KRYLOV_BREAKDOWN; break; }
         const double alpha = rho / r0v[0];
         const float af = (float)alpha;
         // s = r - alpha v ; x += alpha M p ; t = A (M s) ; t.t ; t.s
-        double ts[2] = {0.0, 0.0};
+        ff acct[2] = {ff_zero(), ff_zero()};
         for (int i = i0; i < C; i += stride) {
             float si[3], ti[3];
 #pragma unroll
@@ -234,8 +243,7 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
                 ti[o] = diag[q] * (si[o] * invd[q]);
             }
 #pragma unroll
-    #pragma unroll
-        for (int j = 0; j < W; ++j) {
+            for (int j = 0; j < W; ++j) {
                 const float v = off[(size_t)j * C + i];
                 const int c = col[(size_t)j * C + i];
 #pragma unroll
@@ -250,15 +258,17 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
                 const size_t q = 3 * (size_t)i + o;
                 s[q] = si[o];
                 t[q] = ti[o];
-                ts[0] += (double)ti[o] * ti[o];
-                ts[1] += (double)ti[o] * si[o];
+                ff_fma(acct[0], ti[o], ti[o]);
+                ff_fma(acct[1], ti[o], si[o]);
             }
         }
+        double ts[2];
+        block_reduce_ff<2, BS>(acct, ts);
         SYNC(2, ts);
         const double omega = ts[0] != 0.0 ? ts[1] / ts[0] : 0.0;
         of = (float)omega;
         // x += omega M s ; r = s - omega t ; r.r ; r0.r
-        double rr2[2] = {0.0, 0.0};
+        ff accr[2] = {ff_zero(), ff_zero()};
         for (int i = i0; i < C; i += stride) {
 #pragma unroll
             for (int o = 0; o < 3; ++o) {
@@ -267,10 +277,12 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
                 x[q] += of * (si * invd[q]);
                 const float ri = si - of * t[q];
                 r[q] = ri;
-                rr2[0] += (double)ri * ri;
-                rr2[1] += (double)r0[q] * ri;
+                ff_fma(accr[0], ri, ri);
+                ff_fma(accr[1], r0[q], ri);
             }
         }
+        double rr2[2];
+        block_reduce_ff<2, BS>(accr, rr2);
         SYNC(2, rr2);
         rr = rr2[0];
         ++k;

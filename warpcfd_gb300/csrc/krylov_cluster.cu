@@ -8,9 +8,9 @@
 //    the final write of x.
 //  * Grid-wide synchronisation is the hardware cluster barrier
 //    (barrier.cluster.arrive.release / wait.acquire).  A dot product is an all-reduce: each
-//    CTA sums its rows, stores the block total into a slot of every CTA's shared memory,
-//    and after the barrier every CTA adds the CS slots in rank order, so all CTAs (and all
-//    runs) agree bit for bit.  All CTAs take the same branch at every test, so no CTA can
+//    CTA sums its rows (exact products in float-float, common.cuh), stores its fp64 total
+//    into a slot of every CTA's shared memory, and after the barrier one warp per CTA adds
+//    the CS slots in a fixed order, so all CTAs (and all runs) agree bit for bit.  All CTAs take the same branch at every test, so no CTA can
 //    leave while another still waits or reads its memory.
 //  * The direction update p = z + beta p is evaluated inside the SpMV for the row and its
 //    neighbours (double-buffered p), so an iteration needs two barriers.
@@ -43,32 +43,54 @@ __device__ __forceinline__ uint32_t map_rank(const void* p, unsigned rank) {
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
     return r;
 }
+// Loads stay ordered against the cluster barrier (both are volatile asm) but carry no
+// memory clobber, so the compiler may keep several of them in flight.
 __device__ __forceinline__ float ld_cluster_f32(uint32_t addr) {
     float v;
-    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(addr) : "memory");
+    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(addr));
     return v;
+}
+// value at packed column cp = (rank << 24) | local of an array laid out like `base` in
+// every CTA: a plain shared-memory load when this CTA owns it, a DSMEM load otherwise
+__device__ __forceinline__ float ld_col(const float* base, uint32_t cp, unsigned me) {
+    const unsigned rk = cp >> 24;
+    const uint32_t lo = cp & 0xFFFFFFu;
+    if (rk == me) return base[lo];
+    return ld_cluster_f32(map_rank(base + lo, rk));
 }
 __device__ __forceinline__ void st_cluster_f64(uint32_t addr, double v) {
     asm volatile("st.shared::cluster.f64 [%0], %1;" :: "r"(addr), "d"(v) : "memory");
 }
 
-// all-reduce of NV doubles over the cluster; slots double-buffered by `parity`
+// All-reduce over the cluster of NV float-float accumulators: the CTA total (fp64) is
+// stored into slot `me` of every CTA's shared memory, and after the barrier one warp
+// adds the cs slots in a fixed order, so every CTA gets the same bits.  Slots are
+// double-buffered by `parity`.
 template <int NV>
-__device__ __forceinline__ void cluster_allreduce(double (&v)[NV], double* slots, unsigned parity, unsigned me,
-                                                  unsigned cs) {
-    block_sum<NV, CBS>(v);
+__device__ __forceinline__ void cluster_allreduce(ff (&acc)[NV], double (&out)[NV], double* slots, unsigned parity,
+                                                  unsigned me, unsigned cs) {
+    __shared__ double res[NV];
+    double tot[NV];
+    block_reduce_ff<NV, CBS>(acc, tot);
     double* base = slots + parity * (NV * 16);
     if (threadIdx.x < cs) {
 #pragma unroll
-        for (int i = 0; i < NV; ++i) st_cluster_f64(map_rank(base + i * 16 + me, threadIdx.x), v[i]);
+        for (int i = 0; i < NV; ++i) st_cluster_f64(map_rank(base + i * 16 + me, threadIdx.x), tot[i]);
     }
     cluster_sync_all();
+    if (threadIdx.x < 32) {
+        const unsigned lane = threadIdx.x;
 #pragma unroll
-    for (int i = 0; i < NV; ++i) {
-        double s = 0.0;
-        for (unsigned q = 0; q < cs; ++q) s += base[i * 16 + q];
-        v[i] = s;
+        for (int i = 0; i < NV; ++i) {
+            double x = lane < cs ? base[i * 16 + lane] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane == 0) res[i] = x;
+        }
     }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) out[i] = res[i];
 }
 
 // dynamic shared memory per CTA for R rows and width W:
@@ -111,23 +133,21 @@ __global__ void __launch_bounds__(CBS) cg_cluster_kernel(KrylovArgs a, int R) {
     }
     cluster_sync_all();
     // r = b - A x ; p = z = M r ; rr ; rz
-    double red[2] = {0.0, 0.0};
+    ff acc[2] = {ff_zero(), ff_zero()};
     for (int l = threadIdx.x; l < nloc; l += CBS) {
         float ax = diag[l] * x[l];
 #pragma unroll
-        for (int j = 0; j < W; ++j) {
-            const uint32_t cp = colp[(size_t)j * R + l];
-            ax += off[(size_t)j * R + l] * ld_cluster_f32(map_rank(x + (cp & 0xFFFFFFu), cp >> 24));
-        }
+        for (int j = 0; j < W; ++j) ax += off[(size_t)j * R + l] * ld_col(x, colp[(size_t)j * R + l], me);
         const float ri = a.A.rhs[row0 + l] - ax;
         const float zi = ri * invd[l];
         r[l] = ri;
         pbuf0[l] = zi;
-        red[0] += (double)ri * ri;
-        red[1] += (double)ri * zi;
+        ff_fma(acc[0], ri, ri);
+        ff_fma(acc[1], ri, zi);
     }
     unsigned parity = 0;
-    cluster_allreduce<2>(red, slots, parity, me, cs);
+    double red[2];
+    cluster_allreduce<2>(acc, red, slots, parity, me, cs);
     parity ^= 1u;
     double rr = red[0], rz = red[1];
     float bf = 0.0f;
@@ -135,39 +155,39 @@ __global__ void __launch_bounds__(CBS) cg_cluster_kernel(KrylovArgs a, int R) {
     while (k < a.maxiter && rr > a.atol2) {
         float* po = cur ? pbuf1 : pbuf0;
         float* pn = cur ? pbuf0 : pbuf1;
-        double pq[1] = {0.0};
+        ff accq[1] = {ff_zero()};
         for (int l = threadIdx.x; l < nloc; l += CBS) {
             const float pi = r[l] * invd[l] + bf * po[l];
             float qi = diag[l] * pi;
-    #pragma unroll
-        for (int j = 0; j < W; ++j) {
+#pragma unroll
+            for (int j = 0; j < W; ++j) {
                 const uint32_t cp = colp[(size_t)j * R + l];
-                const unsigned rk = cp >> 24;
-                const uint32_t lo = cp & 0xFFFFFFu;
-                const float rc = ld_cluster_f32(map_rank(r + lo, rk));
-                const float dc = ld_cluster_f32(map_rank(invd + lo, rk));
-                const float pc = ld_cluster_f32(map_rank(po + lo, rk));
+                const float rc = ld_col(r, cp, me);
+                const float dc = ld_col(invd, cp, me);
+                const float pc = ld_col(po, cp, me);
                 qi += off[(size_t)j * R + l] * (rc * dc + bf * pc);
             }
             pn[l] = pi;
             q[l] = qi;
-            pq[0] += (double)pi * qi;
+            ff_fma(accq[0], pi, qi);
         }
-        cluster_allreduce<1>(pq, slots, parity, me, cs);
+        double pq[1];
+        cluster_allreduce<1>(accq, pq, slots, parity, me, cs);
         parity ^= 1u;
         if (pq[0] == 0.0) { status = WCFD_KRYLOV_BREAKDOWN; break; }
         const double alpha = rz / pq[0];
         const float af = (float)alpha;
-        double red2[2] = {0.0, 0.0};
+        ff acc2[2] = {ff_zero(), ff_zero()};
         for (int l = threadIdx.x; l < nloc; l += CBS) {
             x[l] += af * pn[l];
             const float ri = r[l] - af * q[l];
             r[l] = ri;
             const float zi = ri * invd[l];
-            red2[0] += (double)ri * ri;
-            red2[1] += (double)ri * zi;
+            ff_fma(acc2[0], ri, ri);
+            ff_fma(acc2[1], ri, zi);
         }
-        cluster_allreduce<2>(red2, slots, parity, me, cs);
+        double red2[2];
+        cluster_allreduce<2>(acc2, red2, slots, parity, me, cs);
         parity ^= 1u;
         rr = red2[0];
         const double beta = rz != 0.0 ? red2[1] / rz : 0.0;
