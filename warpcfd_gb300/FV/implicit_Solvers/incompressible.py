@@ -97,7 +97,23 @@ class IncompressibleSolver:
                              int(bool(m.skew_correction)), float(self.vel_equation.tol),
                              float(self.p_corr_equation.tol))
 
+    def _param_key(self):
+        m = self.model
+        return (self.material.density, self.material.viscosity, self.steady_state, self.u_relaxation_factor,
+                self.p_relaxation_factor, self.dt, m.reference_pressure_cell_id, m.reference_pressure,
+                self.NUM_INNER_LOOPS, self.NUM_ORTHOGONAL_CORRECTORS, self.vel_equation.max_iter,
+                m.skew_correction, self.vel_equation.tol, self.p_corr_equation.tol, self._events_ptr)
+
     def case_struct(self) -> _lib.Case_t:
+        """The C struct of this case; rebuilt only when a parameter changed (the device
+        arrays never move)."""
+        key = self._param_key()
+        if getattr(self, "_case_key", None) != key:
+            self._case = self._build_case_struct()
+            self._case_key = key
+        return self._case
+
+    def _build_case_struct(self) -> _lib.Case_t:
         m = self.model
         ve, pe = self.vel_equation, self.p_corr_equation
         return _lib.Case_t(self._mesh_t, m.bc_struct(), m.state_struct(), ve.system_struct(), pe.system_struct(),
@@ -108,8 +124,7 @@ class IncompressibleSolver:
     # ------------------------------------------------------------------ stepping
     def step(self):
         """One SIMPLE outer iteration or one PISO time step on the current stream."""
-        case = self.case_struct()
-        _lib.call("wcfd_simple_iteration", ct.byref(case), _stream())
+        _lib.call("wcfd_simple_iteration", ct.byref(self.case_struct()), _stream())
 
     def assemble_momentum(self):
         """Momentum system from the current fields (incompressible.py:102-113) into
@@ -147,9 +162,9 @@ class IncompressibleSolver:
         return self.report(nsteps)
 
     def _graph_step_counted(self):
-        if self._graph is None or bytes(self.case_struct()) != self._graph_key:
+        if self._graph is None or self._param_key() != self._graph_key:
             # first call captures; the capture itself does not execute, so run one eager step
-            key = bytes(self.case_struct())
+            key = self._param_key()
             self.step()
             torch.cuda.synchronize()
             g = torch.cuda.CUDAGraph()

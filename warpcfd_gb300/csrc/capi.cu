@@ -163,12 +163,24 @@ int try_cluster_cg(const wcfd_mesh* m, wcfd_system A, float* x, double atol, int
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    int nclusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&nclusters, fn, &cfg) != cudaSuccess ||
-        nclusters < 1) {
-        cudaGetLastError();
-        return -1;
+    // whether this (device, size, width) cluster launch is schedulable, asked once
+    static std::mutex qmu;
+    struct Q { int dev, C, W, ok; };
+    static Q qcache[32];
+    static int nq = 0;
+    int ok = -1;
+    {
+        std::lock_guard<std::mutex> lk(qmu);
+        for (int i = 0; i < nq; ++i)
+            if (qcache[i].dev == dev && qcache[i].C == C && qcache[i].W == W) ok = qcache[i].ok;
+        if (ok < 0) {
+            int nclusters = 0;
+            ok = (cudaOccupancyMaxActiveClusters(&nclusters, fn, &cfg) == cudaSuccess && nclusters >= 1) ? 1 : 0;
+            cudaGetLastError();
+            if (nq < 32) qcache[nq++] = Q{dev, C, W, ok};
+        }
     }
+    if (!ok) return -1;
     KrylovArgs a = {};
     a.m = *m;
     a.A = A;

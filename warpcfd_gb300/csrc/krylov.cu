@@ -1,8 +1,8 @@
 // Persistent Krylov solvers: one cooperative launch per solve, rows distributed
 // grid-stride over all co-resident blocks, fp64-accurate dot products (exact products
 // summed in float-float within a warp, fp64 across warps and blocks; common.cuh) reduced
-// deterministically at bounded grid barriers.  They replace warp.optim.linear.cg / bicgstab
-// with the diagonal (Jacobi) preconditioner as called by Equation.solve_Axb
+// deterministically at bounded grid barriers.  They replace warp.optim.linear.cg /
+// bicgstab with the diagonal (Jacobi) preconditioner as called by Equation.solve_Axb
 // (warp_cfd/FV/terms/equation.py:195-200).  Stop test: ||r||_2 <= atol before an
 // iteration, or maxiter iterations.
 //
@@ -11,6 +11,11 @@
 // itself and for every gathered neighbour, and the new direction is written to the other
 // half of a double buffer.  The arithmetic is the textbook algorithm's, but a CG iteration
 // needs two grid barriers instead of three and a BiCGSTAB iteration three instead of five.
+//
+// All fp64 scalar work (alpha, beta, omega, the stop test) is done by thread 0 of each
+// block and handed to the other threads through shared memory: GB300 runs fp64 at about
+// 1/64 of its fp32 rate, and an fp64 division in every thread would cost more than the
+// memory traffic of the iteration.
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -19,6 +24,13 @@ namespace wcfd {
 constexpr int BS = kSolverBlock;
 
 __device__ __forceinline__ float jacobi(float d) { return d != 0.0f ? 1.0f / d : 1.0f; }
+
+// Krylov scalars of one block, owned by thread 0
+struct KScalars {
+    double rr, rz, rho, alpha;
+    float af, bf, of;
+    int go, status, k;
+};
 
 // On a failed barrier (timeout, or another block's error) every block leaves; block 0
 // records the error word so the caller sees why the solve stopped.
@@ -30,21 +42,21 @@ __device__ void fail_stats(const KrylovArgs& a, int k) {
     }
 }
 
-#define SYNC(NV, arr)                                   \
-    do {                                                \
-        if (!grid_sync<NV, BS>(a.g, arr, ++phase)) {    \
-            fail_stats(a, k);                           \
-            return;                                     \
-        }                                               \
+#define SYNC(NV, arr)                                      \
+    do {                                                   \
+        if (!grid_sync<NV, BS>(a.g, arr, ++phase)) {       \
+            fail_stats(a, sc.k);                           \
+            return;                                        \
+        }                                                  \
     } while (0)
 
-__device__ void write_stats(const KrylovArgs& a, int k, double rr, int status) {
+__device__ void write_stats(const KrylovArgs& a, const KScalars& sc) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        int st = status;
-        if (st == WCFD_OK && !(rr <= a.atol2)) st = WCFD_NOT_CONVERGED;
-        a.stats->iterations = k;
+        int st = sc.status;
+        if (st == WCFD_OK && !(sc.rr <= a.atol2)) st = WCFD_NOT_CONVERGED;
+        a.stats->iterations = sc.k;
         a.stats->status = st;
-        a.stats->residual = sqrt(rr);
+        a.stats->residual = sqrt(sc.rr);
     }
 }
 
@@ -53,6 +65,7 @@ __device__ void write_stats(const KrylovArgs& a, int k, double rr, int status) {
 // Workspace: r, pA, pB, q, invd (5 C floats).
 template <int W>
 __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
+    __shared__ KScalars sc;
     const int C = a.m.n_cells;
     float* r = a.ws;
     float* pbuf[2] = {a.ws + (size_t)C, a.ws + 2 * (size_t)C};
@@ -66,7 +79,10 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
     const int stride = gridDim.x * BS;
     const int i0 = blockIdx.x * BS + threadIdx.x;
     unsigned phase = 0;
-    int k = 0, status = WCFD_OK;
+    if (threadIdx.x == 0) {
+        sc.k = 0;
+        sc.status = WCFD_OK;
+    }
 
     // r = b - A x ; z = M r ; p = z ; rr = r.r ; rz = r.z
     ff acc[2] = {ff_zero(), ff_zero()};
@@ -86,10 +102,16 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
     double red[2];
     block_reduce_ff<2, BS>(acc, red);
     SYNC(2, red);
-    double rr = red[0], rz = red[1];
-    float bf = 0.0f;  // first direction is z itself
+    if (threadIdx.x == 0) {
+        sc.rr = red[0];
+        sc.rz = red[1];
+        sc.bf = 0.0f;  // the first direction is z itself
+        sc.go = (0 < a.maxiter && red[0] > a.atol2);
+    }
+    __syncthreads();
     int cur = 0;
-    while (k < a.maxiter && rr > a.atol2) {
+    while (sc.go) {
+        const float bf = sc.bf;
         const float* po = pbuf[cur];  // written by other blocks in this launch: no restrict
         float* pn = pbuf[cur ^ 1];
         // p_new = z + beta p_old (here and for every neighbour) ; q = A p_new ; p.q
@@ -109,9 +131,17 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
         double pq[1];
         block_reduce_ff<1, BS>(accq, pq);
         SYNC(1, pq);
-        if (pq[0] == 0.0) { status = WCFD_KRYLOV_BREAKDOWN; break; }
-        const double alpha = rz / pq[0];
-        const float af = (float)alpha;
+        if (threadIdx.x == 0) {
+            if (pq[0] == 0.0) {
+                sc.status = WCFD_KRYLOV_BREAKDOWN;
+                sc.go = 0;
+            } else {
+                sc.af = (float)(sc.rz / pq[0]);
+            }
+        }
+        __syncthreads();
+        if (!sc.go) break;
+        const float af = sc.af;
         // x += alpha p ; r -= alpha q ; rr ; rz
         ff acc2[2] = {ff_zero(), ff_zero()};
         for (int i = i0; i < C; i += stride) {
@@ -125,14 +155,17 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
         double red2[2];
         block_reduce_ff<2, BS>(acc2, red2);
         SYNC(2, red2);
-        rr = red2[0];
-        const double beta = rz != 0.0 ? red2[1] / rz : 0.0;
-        rz = red2[1];
-        bf = (float)beta;
+        if (threadIdx.x == 0) {
+            sc.rr = red2[0];
+            sc.bf = (float)(sc.rz != 0.0 ? red2[1] / sc.rz : 0.0);
+            sc.rz = red2[1];
+            sc.k += 1;
+            sc.go = (sc.k < a.maxiter && sc.rr > a.atol2);
+        }
+        __syncthreads();
         cur ^= 1;
-        ++k;
     }
-    write_stats(a, k, rr, status);
+    write_stats(a, sc);
 }
 
 // Right-preconditioned (Jacobi) BiCGSTAB on the 3-component momentum system
@@ -140,6 +173,7 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
 // Workspace (3C floats each): r, r0, pA, pB, vA, vB, t, s, invd.
 template <int W>
 __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
+    __shared__ KScalars sc;
     const int C = a.m.n_cells;
     const size_t n3 = 3 * (size_t)C;
     float* r = a.ws;
@@ -157,7 +191,10 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
     const int stride = gridDim.x * BS;
     const int i0 = blockIdx.x * BS + threadIdx.x;
     unsigned phase = 0;
-    int k = 0, status = WCFD_OK;
+    if (threadIdx.x == 0) {
+        sc.k = 0;
+        sc.status = WCFD_OK;
+    }
 
     // r = b - A x ; r0 = r ; p = r ; v = 0 ; rr ; rho = r0.r = rr
     ff acc[1] = {ff_zero()};
@@ -187,11 +224,17 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
     double red[1];
     block_reduce_ff<1, BS>(acc, red);
     SYNC(1, red);
-    double rr = red[0];
-    double rho = rr;
-    float bf = 0.0f, of = 0.0f;  // first direction is r itself
+    if (threadIdx.x == 0) {
+        sc.rr = red[0];
+        sc.rho = red[0];
+        sc.bf = 0.0f;  // the first direction is r itself
+        sc.of = 0.0f;
+        sc.go = (0 < a.maxiter && red[0] > a.atol2);
+    }
+    __syncthreads();
     int cur = 0;
-    while (k < a.maxiter && rr > a.atol2) {
+    while (sc.go) {
+        const float bf = sc.bf, of0 = sc.of;
         const float* po = pbuf[cur];  // written by other blocks in this launch: no restrict
         const float* vo = vbuf[cur];
         float* pn = pbuf[cur ^ 1];
@@ -203,7 +246,7 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
 #pragma unroll
             for (int o = 0; o < 3; ++o) {
                 const size_t q = 3 * (size_t)i + o;
-                pi[o] = r[q] + bf * (po[q] - of * vo[q]);
+                pi[o] = r[q] + bf * (po[q] - of0 * vo[q]);
                 vi[o] = diag[q] * (pi[o] * invd[q]);
             }
 #pragma unroll
@@ -213,7 +256,7 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
 #pragma unroll
                 for (int o = 0; o < 3; ++o) {
                     const size_t q = 3 * (size_t)c + o;
-                    const float pc = r[q] + bf * (po[q] - of * vo[q]);
+                    const float pc = r[q] + bf * (po[q] - of0 * vo[q]);
                     vi[o] += v * (pc * invd[q]);
                 }
             }
@@ -228,9 +271,18 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
         double r0v[1];
         block_reduce_ff<1, BS>(accv, r0v);
         SYNC(1, r0v);
-        if (r0v[0] == 0.0) { status = WCFD_KRYLOV_BREAKDOWN; break; }
-        const double alpha = rho / r0v[0];
-        const float af = (float)alpha;
+        if (threadIdx.x == 0) {
+            if (r0v[0] == 0.0) {
+                sc.status = WCFD_KRYLOV_BREAKDOWN;
+                sc.go = 0;
+            } else {
+                sc.alpha = sc.rho / r0v[0];
+                sc.af = (float)sc.alpha;
+            }
+        }
+        __syncthreads();
+        if (!sc.go) break;
+        const float af = sc.af;
         // s = r - alpha v ; x += alpha M p ; t = A (M s) ; t.t ; t.s
         ff acct[2] = {ff_zero(), ff_zero()};
         for (int i = i0; i < C; i += stride) {
@@ -249,8 +301,8 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
 #pragma unroll
                 for (int o = 0; o < 3; ++o) {
                     const size_t q = 3 * (size_t)c + o;
-                    const float sc = r[q] - af * vn[q];
-                    ti[o] += v * (sc * invd[q]);
+                    const float scv = r[q] - af * vn[q];
+                    ti[o] += v * (scv * invd[q]);
                 }
             }
 #pragma unroll
@@ -265,8 +317,9 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
         double ts[2];
         block_reduce_ff<2, BS>(acct, ts);
         SYNC(2, ts);
-        const double omega = ts[0] != 0.0 ? ts[1] / ts[0] : 0.0;
-        of = (float)omega;
+        if (threadIdx.x == 0) sc.of = (float)(ts[0] != 0.0 ? ts[1] / ts[0] : 0.0);
+        __syncthreads();
+        const float of = sc.of;
         // x += omega M s ; r = s - omega t ; r.r ; r0.r
         ff accr[2] = {ff_zero(), ff_zero()};
         for (int i = i0; i < C; i += stride) {
@@ -284,15 +337,23 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
         double rr2[2];
         block_reduce_ff<2, BS>(accr, rr2);
         SYNC(2, rr2);
-        rr = rr2[0];
-        ++k;
-        if (omega == 0.0 || rho == 0.0) { status = WCFD_KRYLOV_BREAKDOWN; break; }
-        const double beta = (rr2[1] / rho) * (alpha / omega);
-        rho = rr2[1];
-        bf = (float)beta;
+        if (threadIdx.x == 0) {
+            const double omega = ts[0] != 0.0 ? ts[1] / ts[0] : 0.0;
+            sc.rr = rr2[0];
+            sc.k += 1;
+            if (omega == 0.0 || sc.rho == 0.0) {
+                sc.status = WCFD_KRYLOV_BREAKDOWN;
+                sc.go = 0;
+            } else {
+                sc.bf = (float)((rr2[1] / sc.rho) * (sc.alpha / omega));
+                sc.rho = rr2[1];
+                sc.go = (sc.k < a.maxiter && sc.rr > a.atol2);
+            }
+        }
+        __syncthreads();
         cur ^= 1;
     }
-    write_stats(a, k, rr, status);
+    write_stats(a, sc);
 }
 
 const void* cg_kernel_for(int W) {

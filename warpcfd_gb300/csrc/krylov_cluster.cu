@@ -101,6 +101,12 @@ template <int W>
 __global__ void __launch_bounds__(CBS) cg_cluster_kernel(KrylovArgs a, int R) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ double slots[2 * 2 * 16];
+    struct Scal {
+        double rr, rz;
+        float af, bf;
+        int go, status, k;
+    };
+    __shared__ Scal sc;
     const int C = a.m.n_cells;
     const unsigned me = cluster_rank();
     const unsigned cs = cluster_nranks();
@@ -115,7 +121,6 @@ __global__ void __launch_bounds__(CBS) cg_cluster_kernel(KrylovArgs a, int R) {
     float* pbuf0 = r + R;
     float* pbuf1 = pbuf0 + R;
     float* q = pbuf1 + R;
-    int k = 0, status = WCFD_OK;
 
     // load this CTA's slice
     for (int l = threadIdx.x; l < nloc; l += CBS) {
@@ -149,10 +154,19 @@ __global__ void __launch_bounds__(CBS) cg_cluster_kernel(KrylovArgs a, int R) {
     double red[2];
     cluster_allreduce<2>(acc, red, slots, parity, me, cs);
     parity ^= 1u;
-    double rr = red[0], rz = red[1];
-    float bf = 0.0f;
+    // fp64 scalar work by thread 0 only (fp64 runs at ~1/64 of the fp32 rate on GB300)
+    if (threadIdx.x == 0) {
+        sc.rr = red[0];
+        sc.rz = red[1];
+        sc.bf = 0.0f;
+        sc.k = 0;
+        sc.status = WCFD_OK;
+        sc.go = (0 < a.maxiter && red[0] > a.atol2);
+    }
+    __syncthreads();
     int cur = 0;
-    while (k < a.maxiter && rr > a.atol2) {
+    while (sc.go) {
+        const float bf = sc.bf;
         float* po = cur ? pbuf1 : pbuf0;
         float* pn = cur ? pbuf0 : pbuf1;
         ff accq[1] = {ff_zero()};
@@ -174,9 +188,17 @@ __global__ void __launch_bounds__(CBS) cg_cluster_kernel(KrylovArgs a, int R) {
         double pq[1];
         cluster_allreduce<1>(accq, pq, slots, parity, me, cs);
         parity ^= 1u;
-        if (pq[0] == 0.0) { status = WCFD_KRYLOV_BREAKDOWN; break; }
-        const double alpha = rz / pq[0];
-        const float af = (float)alpha;
+        if (threadIdx.x == 0) {
+            if (pq[0] == 0.0) {
+                sc.status = WCFD_KRYLOV_BREAKDOWN;
+                sc.go = 0;
+            } else {
+                sc.af = (float)(sc.rz / pq[0]);
+            }
+        }
+        __syncthreads();
+        if (!sc.go) break;
+        const float af = sc.af;
         ff acc2[2] = {ff_zero(), ff_zero()};
         for (int l = threadIdx.x; l < nloc; l += CBS) {
             x[l] += af * pn[l];
@@ -189,20 +211,23 @@ __global__ void __launch_bounds__(CBS) cg_cluster_kernel(KrylovArgs a, int R) {
         double red2[2];
         cluster_allreduce<2>(acc2, red2, slots, parity, me, cs);
         parity ^= 1u;
-        rr = red2[0];
-        const double beta = rz != 0.0 ? red2[1] / rz : 0.0;
-        rz = red2[1];
-        bf = (float)beta;
+        if (threadIdx.x == 0) {
+            sc.rr = red2[0];
+            sc.bf = (float)(sc.rz != 0.0 ? red2[1] / sc.rz : 0.0);
+            sc.rz = red2[1];
+            sc.k += 1;
+            sc.go = (sc.k < a.maxiter && sc.rr > a.atol2);
+        }
+        __syncthreads();
         cur ^= 1;
-        ++k;
     }
     for (int l = threadIdx.x; l < nloc; l += CBS) a.x[row0 + l] = x[l];
     if (me == 0 && threadIdx.x == 0) {
-        int st = status;
-        if (st == WCFD_OK && !(rr <= a.atol2)) st = WCFD_NOT_CONVERGED;
-        a.stats->iterations = k;
+        int st = sc.status;
+        if (st == WCFD_OK && !(sc.rr <= a.atol2)) st = WCFD_NOT_CONVERGED;
+        a.stats->iterations = sc.k;
         a.stats->status = st;
-        a.stats->residual = sqrt(rr);
+        a.stats->residual = sqrt(sc.rr);
     }
 }
 
