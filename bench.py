@@ -34,13 +34,23 @@ WORKLOADS = {
     "channel": "steady channel 400x80x1 hex on 10x1, u_in=1, p_out=0, Re=200, SIMPLE 0.7/0.3, fp32 (fp64 reductions)",
     "cavity": "lid-driven cavity 64x64x1 hex, lid u=1, Re=100, SIMPLE 0.7/0.3, fp32 (fp64 reductions)",
     "cavity3d": "3D lid-driven cavity 128^3 hex, lid u=1, Re=400, SIMPLE 0.7/0.3, fp32 (fp64 reductions)",
+    "cylinder": "cylinder D=0.1 in a 2.2x0.41 channel, 254k jittered hex (O-grid, seed 0), parabolic inlet "
+                "U_max=1.5, Re=100, PISO dt=5e-4 with 2 correctors and non-orthogonal correction, fp32 "
+                "(fp64 reductions); one step = one time step",
 }
 METRIC = "cell-iterations/s"
 
 
 def build_mesh(workload):
-    from warpcfd_gb300.preprocess import Mesh, create_2D_grid, create_3D_grid, define_boundary_walls
+    from warpcfd_gb300.preprocess import (Mesh, create_2D_grid, create_3D_grid, create_cylinder_channel_grid,
+                                          define_boundary_walls, define_cylinder_group)
 
+    if workload == "cylinder":
+        g, info = create_cylinder_channel_grid(scale=1.625, jitter=0.1, seed=0)
+        m = Mesh(g)
+        define_boundary_walls(m)
+        define_cylinder_group(m, info["cylinder"])
+        return m
     if workload == "channel":
         m = Mesh(create_2D_grid((0, 0, 0), 400, 80, 10.0, 1.0, 0.1))
     elif workload == "cavity":
@@ -53,8 +63,34 @@ def build_mesh(workload):
     return m
 
 
-def case_setup(workload):
+def solver_setup(workload):
+    """(steady, u_relax, p_relax, dt, correctors, non-orthogonal correction) of a workload."""
+    if workload == "cylinder":
+        return False, None, None, 5e-4, 2, True
+    return True, 0.7, 0.3, 1.0, 1, False
+
+
+def inlet_profile(mesh, u_max=1.5, height=0.41):
+    """Parabolic inlet u(y) = 4 u_max y (H - y) / H^2 on the '-X' faces, in group order."""
+    ids = mesh.groups["-X"].ids
+    y = mesh._geometry64["face_centroid"][ids, 1]
+    return 4.0 * u_max * y * (height - y) / height ** 2
+
+
+def case_setup(workload, mesh=None):
     """(nu, rho, reference cell, bc function) of a workload."""
+    if workload == "cylinder":
+        u_in = inlet_profile(mesh)
+
+        def bc(b):
+            b.velocity_BC("-X", u=u_in, v=0.0, w=0.0)
+            b.pressure_BC("+X", p=0.0)
+            b.no_slip_wall("-Y")
+            b.no_slip_wall("+Y")
+            b.no_slip_wall("cylinder")
+            b.slip_wall("-Z")
+            b.slip_wall("+Z")
+        return 1e-3, 1.0, None, bc
     if workload == "channel":
         def bc(b):
             b.velocity_BC("-X", u=1.0, v=0.0, w=0.0)
@@ -86,14 +122,18 @@ def build_gpu_case(workload, mesh):
     from warpcfd_gb300.FV import FVM
     from warpcfd_gb300.FV.implicit_Solvers import IncompressibleSolver
 
-    nu, rho, ref, bc = case_setup(workload)
+    nu, rho, ref, bc = case_setup(workload, mesh)
+    steady, ur, pr, dt, ncorr, corr = solver_setup(workload)
     model = FVM(mesh)
     model.material.create_incompressible_newtonian_fluid(viscosity=nu * rho, density=rho)
     if ref is not None:
         model.set_reference_pressure(ref, 0.0)
     bc(model.boundary)
     model.finalize()
-    solver = IncompressibleSolver(model, 0.7, 0.3)
+    solver = IncompressibleSolver(model, ur, pr, correction=corr, steady_state=steady)
+    solver.set_iterations(1, ncorr, 1)
+    if not steady:
+        solver.set_time_stepping(1, dt)
     solver.verbose = False
     return model, solver
 
@@ -103,13 +143,22 @@ def build_oracle_case(workload, mesh, T=np.float32):
     from warpcfd_gb300.FV.boundary import Boundary
     from warpcfd_gb300.FV.field import Field
 
-    nu, rho, ref, bc = case_setup(workload)
+    nu, rho, ref, bc = case_setup(workload, mesh)
     fields = {k: Field(k, i) for i, k in enumerate("uvwp")}
     b = Boundary(fields, mesh.groups, mesh.face_properties.boundary_face_ids)
     bc(b)
     b.check()
+    corr = solver_setup(workload)[5]
     return OracleCase(geometry_from_mesh(mesh), b.boundary_type, b.boundary_values, nu * rho, rho, T=T,
-                      reference_cell=ref)
+                      reference_cell=ref, correction=corr)
+
+
+def oracle_step(oc, workload, n=1):
+    steady, ur, pr, dt, ncorr, _ = solver_setup(workload)
+    if steady:
+        oc.run(ur, pr, n_outer=n, n_inner=ncorr)
+    else:
+        oc.run(None, None, n_outer=1, n_inner=ncorr, steady=False, n_time=n, dt=dt)
 
 
 class ClockSampler:
@@ -168,11 +217,11 @@ def cpu_baseline(workload, mesh, seconds=15.0, warm=3):
     """The oracle (fp32, the same algorithm) on this host: ``warm`` untimed outer
     iterations from zero fields, then as many timed ones as fit in ~``seconds``."""
     oc = build_oracle_case(workload, mesh)
-    oc.run(0.7, 0.3, n_outer=warm)
+    oracle_step(oc, workload, warm)
     t0 = time.perf_counter()
     n = 0
     while True:
-        oc.run(0.7, 0.3, n_outer=1)
+        oracle_step(oc, workload, 1)
         n += 1
         if time.perf_counter() - t0 > seconds:
             break
@@ -188,13 +237,13 @@ def run_reference(args):
         return 0
     mesh = build_mesh(args.workload)
     oc = build_oracle_case(args.workload, mesh)
-    oc.run(0.7, 0.3, n_outer=args.warmup)
+    oracle_step(oc, args.workload, args.warmup)
     # each step is one full outer iteration of the workload; stop early (and say so) if
     # the K steps would not end within --ref-seconds
     t0 = time.perf_counter()
     done = 0
     while done < args.steps:
-        oc.run(0.7, 0.3, n_outer=1)
+        oracle_step(oc, args.workload, 1)
         done += 1
         if time.perf_counter() - t0 > args.ref_seconds:
             break
@@ -317,7 +366,7 @@ def run_ours(args):
                    "(256 MiB write outside the step events)", "parallelism": f"replicas x{world}",
                    "krylov_iters_mean": {"bicgstab": float(k_u.mean()), "cg": float(k_p.mean())}},
         "e2e": e2e,
-        "gpu_launches": 13 * K_,
+        "gpu_launches": (6 + 7 * solver.NUM_INNER_LOOPS) * K_,
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks
                      else "fallback", "traffic": None,

@@ -228,3 +228,37 @@ def test_cg_paths_agree_with_oracle(case):
         assert abs(st["iterations"] - ko) <= max(2, ko // 50), (path, st, ko)
         assert rel_l2(x, xo) < 1e-4, path
     assert rel_l2(out[1][0], out[2][0]) < 1e-4
+
+
+def test_cylinder_piso_with_correction_tracks_oracle():
+    """configs[2] in small: jittered all-hex O-grid around a cylinder, parabolic inlet,
+    PISO with 2 correctors and the non-orthogonal Laplacian correction."""
+    from warpcfd_gb300.preprocess import (Mesh, create_cylinder_channel_grid, define_boundary_walls,
+                                          define_cylinder_group)
+
+    g, info = create_cylinder_channel_grid(scale=0.25, jitter=0.1, seed=5)
+    m = Mesh(g)
+    define_boundary_walls(m)
+    define_cylinder_group(m, info["cylinder"])
+    ids = m.groups["-X"].ids
+    y = m._geometry64["face_centroid"][ids, 1]
+    u_in = 4.0 * 1.5 * y * (0.41 - y) / 0.41 ** 2
+
+    def bc(b):
+        b.velocity_BC("-X", u=u_in, v=0.0, w=0.0)
+        b.pressure_BC("+X", p=0.0)
+        b.no_slip_wall("-Y")
+        b.no_slip_wall("+Y")
+        b.no_slip_wall("cylinder")
+        b.slip_wall("-Z")
+        b.slip_wall("+Z")
+
+    model, solver, oc = make_pair(m, bc, nu=1e-3, ref_cell=None, steady=False, dt=5e-4, correction=True,
+                                  inner=2)
+    for it in range(3):
+        solver.step()
+        oracle_step(oc, None, None, steady=False, dt=5e-4, inner=2)
+        gv = fields(model)
+        for o in (0, 1):
+            assert vel_err(gv, oc.cell_values, o) < 1e-4, (it, o)
+        assert rel_l2(gv[:, 3], oc.cell_values[:, 3]) < 1e-3, it

@@ -115,3 +115,119 @@ def define_boundary_walls(m: Mesh):
         walls[name] = boundary_ids[mask]
     m.add_groups(walls, "face")
     return walls
+
+
+def _merge_nodes(points2d, tol=1e-9):
+    """Unique 2D points (rounded to ``tol``) and the map from input to unique index."""
+    key = np.round(points2d / tol).astype(np.int64)
+    uniq, inv = np.unique(key, axis=0, return_inverse=True)
+    pts = np.zeros((len(uniq), 2))
+    np.add.at(pts, inv.ravel(), points2d)
+    cnt = np.bincount(inv.ravel(), minlength=len(uniq))
+    return pts / cnt[:, None], inv.ravel()
+
+
+def _block(xy):
+    """Quads of a structured (ni+1, nj+1, 2) node block, counter-clockwise."""
+    ni, nj = xy.shape[0] - 1, xy.shape[1] - 1
+    idx = np.arange((ni + 1) * (nj + 1)).reshape(ni + 1, nj + 1)
+    q = np.stack([idx[:-1, :-1], idx[1:, :-1], idx[1:, 1:], idx[:-1, 1:]], axis=-1).reshape(-1, 4)
+    return xy.reshape(-1, 2), q
+
+
+def create_cylinder_channel_grid(scale=1.0, dz=0.01, jitter=0.1, seed=0, length=2.2, height=0.41,
+                                 center=(0.2, 0.2), diameter=0.1, box=0.1):
+    """All-hex 2D-extruded channel ``length`` x ``height`` around a cylinder (one cell thick).
+
+    Nine structured blocks: an O-grid of four quadrants between the cylinder (radius
+    diameter/2) and a square of half-width ``box`` around it, and eight rectangular blocks
+    filling the rest of the channel, all with matching nodes.  ``scale`` = 1.0 gives about
+    96k cells, 1.625 about 254k.  Interior nodes (not on the walls, inlet, outlet or the
+    cylinder) move by up to ``jitter`` of their shortest incident edge, from ``seed``.
+
+    Returns (grid, info) with info['cylinder'] = (cx, cy, r) for grouping the cylinder faces.
+    """
+    cx, cy = center
+    r0 = diameter / 2.0
+    x0, x1, y0, y1 = cx - box, cx + box, cy - box, cy + box
+    h = 2 * box / max(8, int(round(64 * scale)))
+    nB = int(round(2 * box / h))
+    nA = max(2, int(round(x0 / h)))
+    nC = max(2, int(round((length - x1) / h)))
+    na = max(2, int(round(y0 / h)))
+    nc = max(2, int(round((height - y1) / h)))
+    nr = max(4, int(round(32 * scale)))
+    xs = [np.linspace(0.0, x0, nA + 1), np.linspace(x0, x1, nB + 1), np.linspace(x1, length, nC + 1)]
+    ys = [np.linspace(0.0, y0, na + 1), np.linspace(y0, y1, nB + 1), np.linspace(y1, height, nc + 1)]
+    pts_list, quads_list, off = [], [], 0
+    for bi in range(3):
+        for bj in range(3):
+            if bi == 1 and bj == 1:
+                continue
+            X, Y = np.meshgrid(xs[bi], ys[bj], indexing="ij")
+            p, q = _block(np.stack([X, Y], axis=-1))
+            pts_list.append(p)
+            quads_list.append(q + off)
+            off += len(p)
+    # O-grid: quadrant k spans angles [th0, th0 + 90deg]; the outer edge is a box side
+    t = np.linspace(0.0, 1.0, nB + 1)
+    s = np.linspace(0.0, 1.0, nr + 1)
+    s = s ** 1.5                                      # cluster radial cells at the cylinder
+    sides = [  # (angle start, outer edge start point, outer edge end point)
+        (-np.pi / 4, (x1, y0), (x1, y1)),
+        (np.pi / 4, (x1, y1), (x0, y1)),
+        (3 * np.pi / 4, (x0, y1), (x0, y0)),
+        (5 * np.pi / 4, (x0, y0), (x1, y0)),
+    ]
+    for th0, pa, pb in sides:
+        th = th0 + t * (np.pi / 2)
+        inner = np.stack([cx + r0 * np.cos(th), cy + r0 * np.sin(th)], axis=-1)        # (nB+1, 2)
+        outer = np.stack([pa[0] + t * (pb[0] - pa[0]), pa[1] + t * (pb[1] - pa[1])], axis=-1)
+        blk = inner[:, None, :] + s[None, :, None] * (outer - inner)[:, None, :]       # (nB+1, nr+1, 2)
+        # index order (i along the arc, j outward) is clockwise for this orientation:
+        # flip j so quads come out counter-clockwise
+        p, q = _block(blk[:, ::-1, :])
+        pts_list.append(p)
+        quads_list.append(q + off)
+        off += len(p)
+    pts2, inv = _merge_nodes(np.concatenate(pts_list))
+    quads = inv[np.concatenate(quads_list)]
+    # counter-clockwise check (signed area > 0), fix any block with the other orientation
+    P = pts2[quads]
+    area = 0.5 * np.sum(P[:, :, 0] * np.roll(P[:, :, 1], -1, axis=1) - np.roll(P[:, :, 0], -1, axis=1) * P[:, :, 1],
+                        axis=1)
+    quads[area < 0] = quads[area < 0][:, ::-1]
+    if jitter > 0.0:
+        n = len(pts2)
+        e = np.concatenate([quads[:, [0, 1]], quads[:, [1, 2]], quads[:, [2, 3]], quads[:, [3, 0]]])
+        le = np.linalg.norm(pts2[e[:, 0]] - pts2[e[:, 1]], axis=1)
+        hmin = np.full(n, np.inf)
+        np.minimum.at(hmin, e[:, 0], le)
+        np.minimum.at(hmin, e[:, 1], le)
+        rr = np.hypot(pts2[:, 0] - cx, pts2[:, 1] - cy)
+        eps = 1e-9
+        fixed = ((pts2[:, 0] < eps) | (pts2[:, 0] > length - eps) | (pts2[:, 1] < eps) |
+                 (pts2[:, 1] > height - eps) | (np.abs(rr - r0) < 1e-7))
+        rng = np.random.default_rng(seed)
+        d = rng.uniform(-1.0, 1.0, size=(n, 2)) * (jitter * hmin)[:, None]
+        d[fixed] = 0.0
+        pts2 = pts2 + d
+    nn = len(pts2)
+    pts3 = np.concatenate([np.column_stack([pts2, np.zeros(nn)]), np.column_stack([pts2, np.full(nn, dz)])])
+    hexes = np.concatenate([quads, quads + nn], axis=1)
+    cells = np.hstack([np.full((len(hexes), 1), 8), hexes]).ravel()
+    return UnstructuredGrid(cells, np.full(len(hexes), HEXAHEDRON), pts3), {"cylinder": (cx, cy, r0)}
+
+
+def define_cylinder_group(m: Mesh, cylinder, name="cylinder", tol=1e-6):
+    """Group the boundary faces on the cylinder surface: in-plane normal (not the front or
+    back face of a cell) and centroid on the circle."""
+    cx, cy, r0 = cylinder
+    fp, cp = m.face_properties, m.cell_properties
+    b = fp.boundary_face_ids
+    c = m._geometry64["face_centroid"][b]
+    nz = cp.normal[fp.adjacent_cells[b, 0], fp.cell_face_index[b, 0], 2]
+    rr = np.hypot(c[:, 0] - cx, c[:, 1] - cy)
+    ids = b[(np.abs(nz) < 0.5) & (np.abs(rr - r0) < r0 * 0.05 + tol)]
+    m.add_group(name, ids, "face")
+    return ids
