@@ -49,8 +49,10 @@ constexpr uint64_t kBarrierTimeoutNs = 1500ull * 1000ull * 1000ull;
 // exactly as an unevaluated sum h + r (TwoProduct with an FMA) and accumulated in
 // float-float arithmetic (Knuth's TwoSum), the "Dot2" scheme of Ogita, Rump and Oishi,
 // "Accurate sum and dot product", SIAM J. Sci. Comput. 26 (2005): the result is as accurate
-// as if it were computed in twice the working precision.  Per-warp totals are converted to
-// fp64 and every sum across warps, blocks and CTAs is done in fp64 in a fixed order.
+// as if it were computed in twice the working precision.  Totals are merged in float-float
+// across warps, blocks and CTAs in a fixed order (TwoSum merges are exact up to the low
+// word) and converted to fp64 once, by one thread: a full-warp fp64 instruction is itself
+// expensive on GB300.
 // __fmul_rn / __fadd_rn keep the compiler from contracting the error-free transforms.
 struct ff {
     float hi, lo;
@@ -78,42 +80,48 @@ __device__ __forceinline__ void ff_merge(ff& a, const ff& b) {
     a.lo = __fadd_rn(__fadd_rn(a.lo, b.lo), q);
 }
 
-// Block total of NV float-float accumulators as fp64, valid in every thread.
+__device__ __forceinline__ void ff_shfl_merge(ff& v, int o) {
+    ff t;
+    t.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+    t.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+    ff_merge(v, t);
+}
+
+__device__ __forceinline__ double ff_to_double(const ff& v) { return (double)v.hi + (double)v.lo; }
+
+// Block total of NV float-float accumulators, still as float-float (the same bits in every
+// thread).  Warps merge by butterfly shuffles, then warp 0 merges the warp totals; no fp64
+// instruction is issued (a full-warp fp64 instruction is expensive on GB300).
 template <int NV, int BS>
-__device__ __forceinline__ void block_reduce_ff(ff (&v)[NV], double (&out)[NV]) {
-    __shared__ double wsum[NV][BS / 32];
-    __shared__ double res[NV];
+__device__ __forceinline__ void block_reduce_ff(ff (&v)[NV]) {
+    __shared__ ff wsum[NV][BS / 32];
+    __shared__ ff res[NV];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            ff t;
-            t.hi = __shfl_xor_sync(0xffffffffu, v[i].hi, o);
-            t.lo = __shfl_xor_sync(0xffffffffu, v[i].lo, o);
-            ff_merge(v[i], t);
-        }
-        if (lane == 0) wsum[i][wid] = (double)v[i].hi + (double)v[i].lo;
+        for (int o = 16; o > 0; o >>= 1) ff_shfl_merge(v[i], o);
+        if (lane == 0) wsum[i][wid] = v[i];
     }
     __syncthreads();
     if (wid == 0) {
 #pragma unroll
         for (int i = 0; i < NV; ++i) {
-            double x = lane < BS / 32 ? wsum[i][lane] : 0.0;
+            ff x = lane < BS / 32 ? wsum[i][lane] : ff_zero();
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            for (int o = 16; o > 0; o >>= 1) ff_shfl_merge(x, o);
             if (lane == 0) res[i] = x;
         }
     }
     __syncthreads();
 #pragma unroll
-    for (int i = 0; i < NV; ++i) out[i] = res[i];
+    for (int i = 0; i < NV; ++i) v[i] = res[i];
     __syncthreads();
 }
 
 // Grid-wide synchronisation state living in caller-provided global memory.
 //   flags[b]   phase number block b has reached (zeroed before each launch)
-//   partials   [2 phase parities][4 values][WCFD_MAX_BLOCKS] per-block totals
+//   partials   [2 phase parities][4 values][WCFD_MAX_BLOCKS] per-block float-float totals
 struct GridCtl {
     double* partials;
     unsigned* flags;
@@ -121,23 +129,24 @@ struct GridCtl {
 };
 
 // Barrier + reduction over all blocks of a cooperative launch, for phase number `phase`
-// (1, 2, 3, ... in every block).  v[] holds this block's fp64 totals (from
-// block_reduce_ff) and returns the grid-wide sums.  Each block publishes its totals and
-// then its flag with one release store (no atomics); all threads of every block wait for
-// the flags in parallel, then warp 0 adds the totals in block-index order, so every block
-// gets the same bits on every run.  Totals are double-buffered by phase parity: a block can
-// only overwrite a buffer after every block has passed the phase that read it.  Every wait
-// is bounded: on timeout the block sets *err and returns false.
+// (1, 2, 3, ... in every block).  v[] holds this block's float-float totals (from
+// block_reduce_ff); on return out[] holds the grid-wide sums in fp64.  Each block
+// publishes its totals and then its flag with one release store (no atomics); all threads
+// of every block wait for the flags in parallel, then warp 0 merges the totals in a fixed
+// order and one thread converts to fp64, so every block gets the same bits on every run.
+// Totals are double-buffered by phase parity: a block can only overwrite a buffer after
+// every block has passed the phase that read it.  Every wait is bounded: on timeout the
+// block sets *err and returns false.
 template <int NV, int BS>
-__device__ bool grid_sync(const GridCtl& g, double* v, unsigned phase) {
+__device__ bool grid_sync(const GridCtl& g, const ff* v, double* out, unsigned phase) {
     __shared__ int s_fail;
     __shared__ double s_res[NV > 0 ? NV : 1];
     if (threadIdx.x == 0) s_fail = 0;
-    double* pb = g.partials + (size_t)(phase & 1u) * 4 * WCFD_MAX_BLOCKS;
+    float2* pb = reinterpret_cast<float2*>(g.partials) + (size_t)(phase & 1u) * 4 * WCFD_MAX_BLOCKS;
     if constexpr (NV > 0) {
         if (threadIdx.x == 0) {
 #pragma unroll
-            for (int i = 0; i < NV; ++i) pb[i * WCFD_MAX_BLOCKS + blockIdx.x] = v[i];
+            for (int i = 0; i < NV; ++i) pb[i * WCFD_MAX_BLOCKS + blockIdx.x] = make_float2(v[i].hi, v[i].lo);
         }
     }
     __syncthreads();  // this block's writes of the phase happen before its release
@@ -168,16 +177,19 @@ __device__ bool grid_sync(const GridCtl& g, double* v, unsigned phase) {
             const int lane = threadIdx.x;
 #pragma unroll
             for (int i = 0; i < NV; ++i) {
-                double x = 0.0;
-                for (int j = lane; j < (int)gridDim.x; j += 32) x += __ldcg(pb + i * WCFD_MAX_BLOCKS + j);
+                ff x = ff_zero();
+                for (int j = lane; j < (int)gridDim.x; j += 32) {
+                    const float2 t = __ldcg(pb + i * WCFD_MAX_BLOCKS + j);
+                    ff_merge(x, ff{t.x, t.y});
+                }
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-                if (lane == 0) s_res[i] = x;
+                for (int o = 16; o > 0; o >>= 1) ff_shfl_merge(x, o);
+                if (lane == 0) s_res[i] = ff_to_double(x);
             }
         }
         __syncthreads();
 #pragma unroll
-        for (int i = 0; i < NV; ++i) v[i] = s_res[i];
+        for (int i = 0; i < NV; ++i) out[i] = s_res[i];
         __syncthreads();
     }
     return true;

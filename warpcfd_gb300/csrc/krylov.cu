@@ -1,7 +1,7 @@
 // Persistent Krylov solvers: one cooperative launch per solve, rows distributed
 // grid-stride over all co-resident blocks, fp64-accurate dot products (exact products
-// summed in float-float within a warp, fp64 across warps and blocks; common.cuh) reduced
-// deterministically at bounded grid barriers.  They replace warp.optim.linear.cg /
+// summed in float-float across threads, warps and blocks and converted to fp64 once;
+// common.cuh) reduced deterministically at bounded grid barriers.  They replace warp.optim.linear.cg /
 // bicgstab with the diagonal (Jacobi) preconditioner as called by Equation.solve_Axb
 // (warp_cfd/FV/terms/equation.py:195-200).  Stop test: ||r||_2 <= atol before an
 // iteration, or maxiter iterations.
@@ -42,12 +42,15 @@ __device__ void fail_stats(const KrylovArgs& a, int k) {
     }
 }
 
-#define SYNC(NV, arr)                                      \
-    do {                                                   \
-        if (!grid_sync<NV, BS>(a.g, arr, ++phase)) {       \
-            fail_stats(a, sc.k);                           \
-            return;                                        \
-        }                                                  \
+// block-reduce the float-float accumulators `acc` and sum them over the grid into the
+// fp64 array `out` (NV values)
+#define SYNC(NV, acc, out)                                         \
+    do {                                                           \
+        block_reduce_ff<NV, BS>(acc);                              \
+        if (!grid_sync<NV, BS>(a.g, acc, out, ++phase)) {          \
+            fail_stats(a, sc.k);                                   \
+            return;                                                \
+        }                                                          \
     } while (0)
 
 __device__ void write_stats(const KrylovArgs& a, const KScalars& sc) {
@@ -100,8 +103,7 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
         ff_fma(acc[1], ri, zi);
     }
     double red[2];
-    block_reduce_ff<2, BS>(acc, red);
-    SYNC(2, red);
+    SYNC(2, acc, red);
     if (threadIdx.x == 0) {
         sc.rr = red[0];
         sc.rz = red[1];
@@ -129,8 +131,7 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
             ff_fma(accq[0], pi, qi);
         }
         double pq[1];
-        block_reduce_ff<1, BS>(accq, pq);
-        SYNC(1, pq);
+        SYNC(1, accq, pq);
         if (threadIdx.x == 0) {
             if (pq[0] == 0.0) {
                 sc.status = WCFD_KRYLOV_BREAKDOWN;
@@ -153,8 +154,7 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
             ff_fma(acc2[1], ri, zi);
         }
         double red2[2];
-        block_reduce_ff<2, BS>(acc2, red2);
-        SYNC(2, red2);
+        SYNC(2, acc2, red2);
         if (threadIdx.x == 0) {
             sc.rr = red2[0];
             sc.bf = (float)(sc.rz != 0.0 ? red2[1] / sc.rz : 0.0);
@@ -222,8 +222,7 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
         }
     }
     double red[1];
-    block_reduce_ff<1, BS>(acc, red);
-    SYNC(1, red);
+    SYNC(1, acc, red);
     if (threadIdx.x == 0) {
         sc.rr = red[0];
         sc.rho = red[0];
@@ -269,8 +268,7 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
             }
         }
         double r0v[1];
-        block_reduce_ff<1, BS>(accv, r0v);
-        SYNC(1, r0v);
+        SYNC(1, accv, r0v);
         if (threadIdx.x == 0) {
             if (r0v[0] == 0.0) {
                 sc.status = WCFD_KRYLOV_BREAKDOWN;
@@ -315,8 +313,7 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
             }
         }
         double ts[2];
-        block_reduce_ff<2, BS>(acct, ts);
-        SYNC(2, ts);
+        SYNC(2, acct, ts);
         if (threadIdx.x == 0) sc.of = (float)(ts[0] != 0.0 ? ts[1] / ts[0] : 0.0);
         __syncthreads();
         const float of = sc.of;
@@ -335,8 +332,7 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
             }
         }
         double rr2[2];
-        block_reduce_ff<2, BS>(accr, rr2);
-        SYNC(2, rr2);
+        SYNC(2, accr, rr2);
         if (threadIdx.x == 0) {
             const double omega = ts[0] != 0.0 ? ts[1] / ts[0] : 0.0;
             sc.rr = rr2[0];

@@ -58,34 +58,34 @@ __device__ __forceinline__ float ld_col(const float* base, uint32_t cp, unsigned
     if (rk == me) return base[lo];
     return ld_cluster_f32(map_rank(base + lo, rk));
 }
-__device__ __forceinline__ void st_cluster_f64(uint32_t addr, double v) {
-    asm volatile("st.shared::cluster.f64 [%0], %1;" :: "r"(addr), "d"(v) : "memory");
+__device__ __forceinline__ void st_cluster_v2f32(uint32_t addr, float a, float b) {
+    asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" :: "r"(addr), "f"(a), "f"(b) : "memory");
 }
 
-// All-reduce over the cluster of NV float-float accumulators: the CTA total (fp64) is
-// stored into slot `me` of every CTA's shared memory, and after the barrier one warp
-// adds the cs slots in a fixed order, so every CTA gets the same bits.  Slots are
-// double-buffered by `parity`.
+// All-reduce over the cluster of NV float-float accumulators: the CTA total is stored
+// into slot `me` of every CTA's shared memory, and after the barrier warp 0 of each CTA
+// merges the cs slots in a fixed order and one thread converts to fp64, so every CTA gets
+// the same bits.  Slots are double-buffered by `parity`.
 template <int NV>
-__device__ __forceinline__ void cluster_allreduce(ff (&acc)[NV], double (&out)[NV], double* slots, unsigned parity,
+__device__ __forceinline__ void cluster_allreduce(ff (&acc)[NV], double (&out)[NV], ff* slots, unsigned parity,
                                                   unsigned me, unsigned cs) {
     __shared__ double res[NV];
-    double tot[NV];
-    block_reduce_ff<NV, CBS>(acc, tot);
-    double* base = slots + parity * (NV * 16);
+    block_reduce_ff<NV, CBS>(acc);
+    ff* base = slots + parity * (NV * 16);
     if (threadIdx.x < cs) {
 #pragma unroll
-        for (int i = 0; i < NV; ++i) st_cluster_f64(map_rank(base + i * 16 + me, threadIdx.x), tot[i]);
+        for (int i = 0; i < NV; ++i)
+            st_cluster_v2f32(map_rank(base + i * 16 + me, threadIdx.x), acc[i].hi, acc[i].lo);
     }
     cluster_sync_all();
     if (threadIdx.x < 32) {
         const unsigned lane = threadIdx.x;
 #pragma unroll
         for (int i = 0; i < NV; ++i) {
-            double x = lane < cs ? base[i * 16 + lane] : 0.0;
+            ff x = lane < cs ? base[i * 16 + lane] : ff_zero();
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-            if (lane == 0) res[i] = x;
+            for (int o = 16; o > 0; o >>= 1) ff_shfl_merge(x, o);
+            if (lane == 0) res[i] = ff_to_double(x);
         }
     }
     __syncthreads();
@@ -100,7 +100,7 @@ size_t cluster_cg_smem_bytes(int R, int W) { return (size_t)R * (8 * (size_t)W +
 template <int W>
 __global__ void __launch_bounds__(CBS) cg_cluster_kernel(KrylovArgs a, int R) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ double slots[2 * 2 * 16];
+    __shared__ ff slots[2 * 2 * 16];
     struct Scal {
         double rr, rz;
         float af, bf;
