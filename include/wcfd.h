@@ -240,6 +240,35 @@ int wcfd_cg_noalloc(const wcfd_mesh* m, wcfd_system A, float* x, double atol, in
  * fused kernels on `stream`; capturable in a CUDA graph. */
 int wcfd_simple_iteration(const wcfd_case* c, void* stream);
 
+/* ------------------------------------------------------------------ batched form
+ * Many cases in one launch per kernel: `cases` is a DEVICE array of wcfd_case (a case
+ * table; each entry points at that case's own arrays).  Field and assembly kernels run
+ * over (case, face/cell) grids; each case's momentum BiCGSTAB and pressure CG run on one
+ * thread-block cluster of `cluster_size` CTAs (the CG out of the cluster's shared memory).
+ * Every case of a batch must have the same faces_per_cell and ell_width; loop counts are
+ * the batch's.  Per-case outcomes go to each case's stats[0..1]. */
+typedef struct wcfd_batch_dims {
+    int32_t max_cells;       /* largest n_cells in the table           */
+    int32_t max_faces;       /* largest n_faces in the table           */
+    int32_t faces_per_cell;  /* common to every case                   */
+    int32_t ell_width;       /* common to every case                   */
+    int32_t n_inner;         /* pressure correctors                    */
+    int32_t n_ortho;         /* non-orthogonal correctors              */
+    int32_t cluster_size;    /* CTAs per case for the solves; 0 = pick */
+    int32_t pad_;
+} wcfd_batch_dims;
+
+/* Cluster size wcfd_batch_simple_iteration would pick for these dims (0 = no cluster
+ * configuration fits: max_cells too large for the cluster-resident CG). */
+int wcfd_batch_cluster_size(const wcfd_batch_dims* dims);
+
+/* One SIMPLE outer iteration (or PISO step) of every case in the table
+ * (incompressible.py:95-156 for each case). */
+int wcfd_batch_simple_iteration(const wcfd_case* cases, int32_t n_cases, const wcfd_batch_dims* dims,
+                                void* stream);
+/* Message of the last failed batched call on this thread. */
+const char* wcfd_batch_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -253,8 +253,11 @@ def test_cylinder_piso_with_correction_tracks_oracle():
         b.slip_wall("-Z")
         b.slip_wall("+Z")
 
+    # at the reference's atol (1e-5) this pressure solve stops far from its solution (|p|
+    # 208 vs 78 converged) and fp32/fp64 oracle runs already differ by 3%, so both sides
+    # solve to atol 1e-7 here
     model, solver, oc = make_pair(m, bc, nu=1e-3, ref_cell=None, steady=False, dt=5e-4, correction=True,
-                                  inner=2)
+                                  inner=2, atol=1e-7)
     for it in range(3):
         solver.step()
         oracle_step(oc, None, None, steady=False, dt=5e-4, inner=2)

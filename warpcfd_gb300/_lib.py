@@ -72,6 +72,12 @@ class Case_t(ct.Structure):
                 ("events", vp)]
 
 
+class BatchDims_t(ct.Structure):
+    _fields_ = [("max_cells", ct.c_int32), ("max_faces", ct.c_int32), ("faces_per_cell", ct.c_int32),
+                ("ell_width", ct.c_int32), ("n_inner", ct.c_int32), ("n_ortho", ct.c_int32),
+                ("cluster_size", ct.c_int32), ("pad_", ct.c_int32)]
+
+
 # name -> (restype, argtypes)
 _SIGS = {
     "wcfd_version": (ct.c_int, []),
@@ -92,6 +98,10 @@ _SIGS = {
     "wcfd_bicgstab": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, KrylovWS_t, ct.c_double, ct.c_int32, vp, vp]),
     "wcfd_simple_iteration": (ct.c_int, [ct.POINTER(Case_t), vp]),
     "wcfd_set_krylov_path": (ct.c_int, [ct.c_int32]),
+    "wcfd_cg_noalloc": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, ct.c_double, ct.c_int32, vp, vp]),
+    "wcfd_batch_cluster_size": (ct.c_int, [ct.POINTER(BatchDims_t)]),
+    "wcfd_batch_simple_iteration": (ct.c_int, [vp, ct.c_int32, ct.POINTER(BatchDims_t), vp]),
+    "wcfd_batch_last_error": (ct.c_char_p, []),
 }
 
 EXPORTED = tuple(_SIGS.keys())

@@ -24,11 +24,7 @@ namespace wcfd {
 //   rUA = V / (diag_u rho) (solver_kernels.py:6-16)
 // Internal-face explicit weights never reach the RHS (equation_kernels.py:84-101), so
 // none are formed here.
-__global__ void __launch_bounds__(kBlock) momentum_assemble_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s,
-                                                                   wcfd_system sys, float* __restrict__ rua,
-                                                                   wcfd_params prm) {
-    const int c = blockIdx.x * kBlock + threadIdx.x;
-    if (c >= m.n_cells) return;
+__device__ __forceinline__ void momentum_assemble_body(const wcfd_mesh& m, const wcfd_bc& bc, const wcfd_state& s, const wcfd_system& sys, float* __restrict__ rua, const wcfd_params& prm, int c) {
     const int C = m.n_cells;
     const float nu = prm.nu;
     float dsum = 0.0f;
@@ -102,18 +98,21 @@ __global__ void __launch_bounds__(kBlock) momentum_assemble_kernel(wcfd_mesh m, 
     rua[c] = V / (d[0] * prm.rho);
 }
 
+__global__ void __launch_bounds__(kBlock) momentum_assemble_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s,
+                                                                   wcfd_system sys, float* __restrict__ rua,
+                                                                   wcfd_params prm) {
+    const int c = blockIdx.x * kBlock + threadIdx.x;
+    if (c >= m.n_cells) return;
+    momentum_assemble_body(m, bc, s, sys, rua, prm, c);
+}
+
 // Pressure row of cell c: DiffusionTerm('p', nu = rUA_f), scale +1 (diffusion.py:113-198)
 //   internal:          diag -= rUA_f A/d ; off = +rUA_f A/d
 //   boundary value:    diag -= rUA_f A/|r_Pf| ; rhs -= rUA_f A/|r_Pf| p_b
 //   boundary gradient: rhs -= rUA_f g A
 // then rhs += div(HbyA) (incompressible.py:137) and, for the reference cell, the row
 // becomes identity with rhs = value (equation_kernels.py:155-175; its column stays).
-__global__ void __launch_bounds__(kBlock) pressure_assemble_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s,
-                                                                   wcfd_system sys,
-                                                                   const float* __restrict__ rua_faces,
-                                                                   const float* __restrict__ div, wcfd_params prm) {
-    const int c = blockIdx.x * kBlock + threadIdx.x;
-    if (c >= m.n_cells) return;
+__device__ __forceinline__ void pressure_assemble_body(const wcfd_mesh& m, const wcfd_bc& bc, const wcfd_state& s, const wcfd_system& sys, const float* __restrict__ rua_faces, const float* __restrict__ div, const wcfd_params& prm, int c) {
     const int C = m.n_cells;
     float d = 0.0f, b = 0.0f;
     int j = 0;
@@ -150,6 +149,15 @@ __global__ void __launch_bounds__(kBlock) pressure_assemble_kernel(wcfd_mesh m, 
     sys.rhs[c] = b;
 }
 
+__global__ void __launch_bounds__(kBlock) pressure_assemble_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s,
+                                                                   wcfd_system sys,
+                                                                   const float* __restrict__ rua_faces,
+                                                                   const float* __restrict__ div, wcfd_params prm) {
+    const int c = blockIdx.x * kBlock + threadIdx.x;
+    if (c >= m.n_cells) return;
+    pressure_assemble_body(m, bc, s, sys, rua_faces, div, prm, c);
+}
+
 // y = A x on the mesh pattern; NC = 1 (scalar) or 3 (momentum: shared off-diagonals,
 // interleaved components).
 template <int NC>
@@ -176,6 +184,25 @@ void launch_spmv(const wcfd_mesh& m, wcfd_system A, const float* x, float* y, cu
         spmv_kernel<1><<<grid_for(m.n_cells), kBlock, 0, st>>>(m, A, x, y);
     else
         spmv_kernel<3><<<grid_for(m.n_cells), kBlock, 0, st>>>(m, A, x, y);
+}
+
+}  // namespace wcfd
+
+// Batched assembly over a device case table (blockIdx.y = case).
+namespace wcfd {
+
+__global__ void __launch_bounds__(kBlock) momentum_assemble_batched(const wcfd_case* __restrict__ cases) {
+    const wcfd_case& c = cases[blockIdx.y];
+    const int i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= c.mesh.n_cells) return;
+    momentum_assemble_body(c.mesh, c.bc, c.state, c.mom, c.rua, c.prm, i);
+}
+
+__global__ void __launch_bounds__(kBlock) pressure_assemble_batched(const wcfd_case* __restrict__ cases) {
+    const wcfd_case& c = cases[blockIdx.y];
+    const int i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= c.mesh.n_cells) return;
+    pressure_assemble_body(c.mesh, c.bc, c.state, c.pres, c.rua_faces, c.div, c.prm, i);
 }
 
 }  // namespace wcfd

@@ -1,0 +1,163 @@
+// Host side of the batched form: one SIMPLE outer iteration (or PISO step) for every case
+// of a device case table, as a fixed sequence of batched launches (capturable in a CUDA
+// graph: the sequence depends only on the dims, never on the data).
+#include <cstdio>
+#include <mutex>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+using namespace wcfd;
+
+namespace {
+
+thread_local char g_batch_error[256] = "";
+
+inline cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+int batch_budget_rows(int W) {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const long long budget = (long long)optin - 4096;  // static shared memory and reserve
+    return budget > 0 ? (int)(budget / (8LL * W + 24)) : 0;
+}
+
+int pick_cluster(const wcfd_batch_dims& d) {
+    const int rmax = batch_budget_rows(d.ell_width);
+    for (int c = 1; c <= 16; c *= 2) {
+        const long long r = (d.max_cells + c - 1) / c;
+        if (r <= rmax && (r <= 2048 || c == 16)) return c;
+    }
+    return 0;
+}
+
+int launch_cluster(const void* fn, int n_cases, int cs, size_t smem, cudaStream_t st, void** args) {
+    static std::mutex mu;
+    static size_t set_bytes[64] = {0};
+    static const void* set_fn[64] = {nullptr};
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        int slot = -1;
+        for (int i = 0; i < 64; ++i)
+            if (set_fn[i] == fn || set_fn[i] == nullptr) {
+                slot = i;
+                break;
+            }
+        if (slot < 0) return WCFD_ERR_CUDA;
+        if (set_fn[slot] == nullptr || set_bytes[slot] < smem) {
+            if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+                cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+                std::snprintf(g_batch_error, sizeof(g_batch_error), "cluster kernel attributes: %s",
+                              cudaGetErrorString(cudaGetLastError()));
+                return WCFD_ERR_CUDA;
+            }
+            set_fn[slot] = fn;
+            set_bytes[slot] = smem;
+        }
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(n_cases * cs);
+    cfg.blockDim = dim3(kClusterBlock);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cs;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelExC(&cfg, fn, args);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        std::snprintf(g_batch_error, sizeof(g_batch_error), "batched cluster launch: %s", cudaGetErrorString(e));
+        return WCFD_ERR_CUDA;
+    }
+    return WCFD_OK;
+}
+
+#define BCHECK(what)                                                                               \
+    do {                                                                                           \
+        const cudaError_t e_ = cudaGetLastError();                                                 \
+        if (e_ != cudaSuccess) {                                                                   \
+            std::snprintf(g_batch_error, sizeof(g_batch_error), "%s: %s", what, cudaGetErrorString(e_)); \
+            return WCFD_ERR_CUDA;                                                                  \
+        }                                                                                          \
+    } while (0)
+
+}  // namespace
+
+extern "C" const char* wcfd_batch_last_error(void) { return g_batch_error; }
+
+extern "C" int wcfd_batch_cluster_size(const wcfd_batch_dims* dims) {
+    if (!dims || dims->max_cells <= 0 || dims->ell_width < 0 || dims->ell_width > kMaxSlots) return 0;
+    return pick_cluster(*dims);
+}
+
+extern "C" int wcfd_batch_simple_iteration(const wcfd_case* cases, int32_t n_cases, const wcfd_batch_dims* dims,
+                                           void* stream) {
+    if (!cases || !dims || n_cases <= 0) {
+        std::snprintf(g_batch_error, sizeof(g_batch_error), "null case table, dims or empty batch");
+        return WCFD_ERR_ARGUMENT;
+    }
+    const wcfd_batch_dims d = *dims;
+    if (d.max_cells <= 0 || d.max_faces <= 0 || d.faces_per_cell < 1 || d.faces_per_cell > kMaxSlots ||
+        d.ell_width < 0 || d.ell_width > d.faces_per_cell || d.n_inner < 0 || d.n_ortho < 0 || n_cases > 65535) {
+        std::snprintf(g_batch_error, sizeof(g_batch_error), "bad batch dims");
+        return WCFD_ERR_ARGUMENT;
+    }
+    const int cs = d.cluster_size > 0 ? d.cluster_size : pick_cluster(d);
+    if (cs < 1 || cs > 16) {
+        std::snprintf(g_batch_error, sizeof(g_batch_error), "no cluster size fits max_cells %d", d.max_cells);
+        return WCFD_ERR_TOO_LARGE;
+    }
+    const int R = (d.max_cells + cs - 1) / cs;
+    if (R > batch_budget_rows(d.ell_width)) {
+        std::snprintf(g_batch_error, sizeof(g_batch_error), "max_cells %d too large for cluster size %d", d.max_cells, cs);
+        return WCFD_ERR_TOO_LARGE;
+    }
+    const void* cg_fn = cg_cluster_batched_for(d.ell_width);
+    const void* bi_fn = bicgstab_cluster_batched_for(d.ell_width);
+    if (!cg_fn || !bi_fn) return WCFD_ERR_ARGUMENT;
+    cudaStream_t st = S(stream);
+    const dim3 gf(grid_for(d.max_faces), n_cases), gc(grid_for(d.max_cells), n_cases);
+    // incompressible.py:96-99
+    face_pass_batched<<<gf, kBlock, 0, st>>>(cases, WCFD_ALL, 1u | 2u);
+    BCHECK("face_pass_batched");
+    gradient_batched<<<gc, kBlock, 0, st>>>(cases, WCFD_ALL, 0);
+    BCHECK("gradient_batched");
+    // :102-116
+    momentum_assemble_batched<<<gc, kBlock, 0, st>>>(cases);
+    BCHECK("momentum_assemble_batched");
+    int csv = cs;
+    void* bargs[] = {(void*)&cases, &csv};
+    int rc = launch_cluster(bi_fn, n_cases, cs, 0, st, bargs);
+    if (rc) return rc;
+    // :118-123
+    hbya_batched<<<gc, kBlock, 0, st>>>(cases);
+    BCHECK("hbya_batched");
+    rua_faces_batched<<<gf, kBlock, 0, st>>>(cases);
+    BCHECK("rua_faces_batched");
+    const size_t smem = cluster_cg_smem_bytes(R, d.ell_width);
+    for (int inner = 0; inner < d.n_inner; ++inner) {
+        for (int ortho = 0; ortho < d.n_ortho; ++ortho) {
+            face_pass_batched<<<gf, kBlock, 0, st>>>(cases, WCFD_ALL, 2u);
+            BCHECK("face_pass_batched");
+            gradient_batched<<<gc, kBlock, 0, st>>>(cases, WCFD_ALL, 1);
+            BCHECK("gradient_batched");
+            pressure_assemble_batched<<<gc, kBlock, 0, st>>>(cases);
+            BCHECK("pressure_assemble_batched");
+            void* cargs[] = {(void*)&cases, &csv};
+            rc = launch_cluster(cg_fn, n_cases, cs, smem, st, cargs);
+            if (rc) return rc;
+            p_update_batched<<<gc, kBlock, 0, st>>>(cases);
+            BCHECK("p_update_batched");
+            face_pass_batched<<<gf, kBlock, 0, st>>>(cases, WCFD_P, 0u);
+            BCHECK("face_pass_batched");
+            gradient_batched<<<gc, kBlock, 0, st>>>(cases, WCFD_P, 2);
+            BCHECK("gradient_batched");
+        }
+    }
+    return WCFD_OK;
+}

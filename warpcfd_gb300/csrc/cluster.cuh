@@ -1,0 +1,82 @@
+// Thread-block-cluster primitives shared by the cluster-resident solvers: rank queries,
+// the hardware cluster barrier, distributed-shared-memory loads and stores, and a
+// deterministic float-float all-reduce over the CTAs of a cluster.
+#pragma once
+
+#include "common.cuh"
+
+namespace wcfd {
+
+constexpr int CBS = kClusterBlock;
+
+__device__ __forceinline__ unsigned cluster_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned cluster_nranks() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+// shared::cluster address of `p` (a pointer into this CTA's shared memory) in CTA `rank`
+__device__ __forceinline__ uint32_t map_rank(const void* p, unsigned rank) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
+// Loads stay ordered against the cluster barrier (both are volatile asm) but carry no
+// memory clobber, so the compiler may keep several of them in flight.
+__device__ __forceinline__ float ld_cluster_f32(uint32_t addr) {
+    float v;
+    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(addr));
+    return v;
+}
+// value at packed column cp = (rank << 24) | local of an array laid out like `base` in
+// every CTA: a plain shared-memory load when this CTA owns it, a DSMEM load otherwise
+__device__ __forceinline__ float ld_col(const float* base, uint32_t cp, unsigned me) {
+    const unsigned rk = cp >> 24;
+    const uint32_t lo = cp & 0xFFFFFFu;
+    if (rk == me) return base[lo];
+    return ld_cluster_f32(map_rank(base + lo, rk));
+}
+__device__ __forceinline__ void st_cluster_v2f32(uint32_t addr, float a, float b) {
+    asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" :: "r"(addr), "f"(a), "f"(b) : "memory");
+}
+
+// All-reduce over the cluster of NV float-float accumulators: the CTA total is stored
+// into slot `me` of every CTA's shared memory, and after the barrier warp 0 of each CTA
+// merges the cs slots in a fixed order and one thread converts to fp64, so every CTA gets
+// the same bits.  Slots are double-buffered by `parity`.
+template <int NV>
+__device__ __forceinline__ void cluster_allreduce(ff (&acc)[NV], double (&out)[NV], ff* slots, unsigned parity,
+                                                  unsigned me, unsigned cs) {
+    __shared__ double res[NV];
+    block_reduce_ff<NV, CBS>(acc);
+    ff* base = slots + parity * (NV * 16);
+    if (threadIdx.x < cs) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i)
+            st_cluster_v2f32(map_rank(base + i * 16 + me, threadIdx.x), acc[i].hi, acc[i].lo);
+    }
+    cluster_sync_all();
+    if (threadIdx.x < 32) {
+        const unsigned lane = threadIdx.x;
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            ff x = lane < cs ? base[i * 16 + lane] : ff_zero();
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) ff_shfl_merge(x, o);
+            if (lane == 0) res[i] = ff_to_double(x);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) out[i] = res[i];
+}
+
+}  // namespace wcfd

@@ -17,10 +17,7 @@ namespace wcfd {
 //        bit1 recompute the mass flux, bit2 skew correction, bit3 upwind instead of
 //        linear interpolation on internal faces (phi_P if mdot > 0 else phi_N,
 //        interpolation_functions.py:18-28; used by face_interpolation(upwind=True)).
-__global__ void __launch_bounds__(kBlock) face_pass_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s,
-                                                           uint32_t mask, uint32_t flags) {
-    const int k = blockIdx.x * kBlock + threadIdx.x;
-    if (k >= m.n_faces) return;
+__device__ __forceinline__ void face_pass_body(const wcfd_mesh& m, const wcfd_bc& bc, const wcfd_state& s, uint32_t mask, uint32_t flags, int k) {
     const int P = __ldg(m.face_owner + k);
     const int N = __ldg(m.face_nbr + k);
     float4 fv = ld4(s.face_values + 4 * (size_t)k);
@@ -73,16 +70,20 @@ __global__ void __launch_bounds__(kBlock) face_pass_kernel(wcfd_mesh m, wcfd_bc 
     }
 }
 
+__global__ void __launch_bounds__(kBlock) face_pass_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s,
+                                                           uint32_t mask, uint32_t flags) {
+    const int k = blockIdx.x * kBlock + threadIdx.x;
+    if (k >= m.n_faces) return;
+    face_pass_body(m, bc, s, mask, flags, k);
+}
+
 // Green-Gauss gradient (model.py:232-239, model_kernels.py:71-90):
 //   grad phi_c = sum_f phi_f A_f n_cf / V_c, gathered per cell in slot order.
 // Fields outside `mask` get a zero gradient (the reference zeroes the whole array).
 // With `div` != null also div[c] = sum_f (+-) mdot_f (model_kernels.py:26-34).
 // With `corr` != null (the pressure correction of incompressible.py:150-156) also
 //   HbyA[c] -= rUA[c] grad p ; cell u,v,w = HbyA.
-__global__ void __launch_bounds__(kBlock) gradient_kernel(wcfd_mesh m, wcfd_state s, uint32_t mask,
-                                                          float* __restrict__ div, CorrectArgs corr) {
-    const int c = blockIdx.x * kBlock + threadIdx.x;
-    if (c >= m.n_cells) return;
+__device__ __forceinline__ void gradient_body(const wcfd_mesh& m, const wcfd_state& s, uint32_t mask, float* __restrict__ div, const CorrectArgs& corr, int c) {
     const int C = m.n_cells;
     float g[4][3];
 #pragma unroll
@@ -124,20 +125,28 @@ __global__ void __launch_bounds__(kBlock) gradient_kernel(wcfd_mesh m, wcfd_stat
     }
 }
 
+__global__ void __launch_bounds__(kBlock) gradient_kernel(wcfd_mesh m, wcfd_state s, uint32_t mask,
+                                                          float* __restrict__ div, CorrectArgs corr) {
+    const int c = blockIdx.x * kBlock + threadIdx.x;
+    if (c >= m.n_cells) return;
+    gradient_body(m, s, mask, div, corr, c);
+}
+
 // mdot = (u_f, v_f, w_f) . n_owner * A (model_kernels.py:45-60)
-__global__ void __launch_bounds__(kBlock) mass_flux_kernel(wcfd_mesh m, wcfd_state s) {
-    const int k = blockIdx.x * kBlock + threadIdx.x;
-    if (k >= m.n_faces) return;
+__device__ __forceinline__ void mass_flux_body(const wcfd_mesh& m, const wcfd_state& s, int k) {
     const float4 fv = ld4(s.face_values + 4 * (size_t)k);
     const float4 n = __ldg(reinterpret_cast<const float4*>(m.face_normal) + k);
     s.mass_fluxes[k] = (fv.x * n.x + fv.y * n.y + fv.z * n.z) * n.w;
 }
 
+__global__ void __launch_bounds__(kBlock) mass_flux_kernel(wcfd_mesh m, wcfd_state s) {
+    const int k = blockIdx.x * kBlock + threadIdx.x;
+    if (k >= m.n_faces) return;
+    mass_flux_body(m, s, k);
+}
+
 // div[c] = sum over the cell's faces of +mdot (owner side) or -mdot (model_kernels.py:26-34)
-__global__ void __launch_bounds__(kBlock) div_kernel(wcfd_mesh m, const float* __restrict__ mdot,
-                                                     float* __restrict__ div) {
-    const int c = blockIdx.x * kBlock + threadIdx.x;
-    if (c >= m.n_cells) return;
+__device__ __forceinline__ void div_body(const wcfd_mesh& m, const float* __restrict__ mdot, float* __restrict__ div, int c) {
     const int C = m.n_cells;
     const float4* slots = reinterpret_cast<const float4*>(m.cell_slot);
     float dv = 0.0f;
@@ -149,11 +158,15 @@ __global__ void __launch_bounds__(kBlock) div_kernel(wcfd_mesh m, const float* _
     div[c] = dv;
 }
 
+__global__ void __launch_bounds__(kBlock) div_kernel(wcfd_mesh m, const float* __restrict__ mdot,
+                                                     float* __restrict__ div) {
+    const int c = blockIdx.x * kBlock + threadIdx.x;
+    if (c >= m.n_cells) return;
+    div_body(m, mdot, div, c);
+}
+
 // interpolate_cell_value_to_face (solver_kernels.py:21-36)
-__global__ void __launch_bounds__(kBlock) cell_to_face_kernel(wcfd_mesh m, const float* __restrict__ x,
-                                                              float* __restrict__ y) {
-    const int k = blockIdx.x * kBlock + threadIdx.x;
-    if (k >= m.n_faces) return;
+__device__ __forceinline__ void cell_to_face_body(const wcfd_mesh& m, const float* __restrict__ x, float* __restrict__ y, int k) {
     const int P = __ldg(m.face_owner + k);
     const int N = __ldg(m.face_nbr + k);
     if (N < 0) {
@@ -164,14 +177,17 @@ __global__ void __launch_bounds__(kBlock) cell_to_face_kernel(wcfd_mesh m, const
     }
 }
 
+__global__ void __launch_bounds__(kBlock) cell_to_face_kernel(wcfd_mesh m, const float* __restrict__ x,
+                                                              float* __restrict__ y) {
+    const int k = blockIdx.x * kBlock + threadIdx.x;
+    if (k >= m.n_faces) return;
+    cell_to_face_body(m, x, y, k);
+}
+
 // After the momentum solve (incompressible.py:118-123):
 //   HbyA += rUA grad p ; cell u,v,w = HbyA.
 // Optionally rUA_f as in cell_to_face for the faces of the same index range.
-__global__ void __launch_bounds__(kBlock) hbya_kernel(int C, const float* __restrict__ grad,
-                                                      const float* __restrict__ rua, float* __restrict__ hbya,
-                                                      float* __restrict__ cell_values) {
-    const int c = blockIdx.x * kBlock + threadIdx.x;
-    if (c >= C) return;
+__device__ __forceinline__ void hbya_body(int C, const float* __restrict__ grad, const float* __restrict__ rua, float* __restrict__ hbya, float* __restrict__ cell_values, int c) {
     const float r = rua[c];
     const float* gp = grad + 12 * (size_t)c + 9;
     float* h = hbya + 3 * (size_t)c;
@@ -183,14 +199,73 @@ __global__ void __launch_bounds__(kBlock) hbya_kernel(int C, const float* __rest
     cv[0] = hx; cv[1] = hy; cv[2] = hz;
 }
 
+__global__ void __launch_bounds__(kBlock) hbya_kernel(int C, const float* __restrict__ grad,
+                                                      const float* __restrict__ rua, float* __restrict__ hbya,
+                                                      float* __restrict__ cell_values) {
+    const int c = blockIdx.x * kBlock + threadIdx.x;
+    if (c >= C) return;
+    hbya_body(C, grad, rua, hbya, cell_values, c);
+}
+
 // p = alpha p_new + (1 - alpha) p (model.py:381-384), or p = p_new (alpha <= 0).
+__device__ __forceinline__ void p_update_body(int C, const float* __restrict__ p_new, float* __restrict__ cell_values, float alpha, int c) {
+    float* p = cell_values + 4 * (size_t)c + 3;
+    if (alpha > 0.0f) *p = alpha * p_new[c] + (1.0f - alpha) * *p;
+    else *p = p_new[c];
+}
+
 __global__ void __launch_bounds__(kBlock) p_update_kernel(int C, const float* __restrict__ p_new,
                                                           float* __restrict__ cell_values, float alpha) {
     const int c = blockIdx.x * kBlock + threadIdx.x;
     if (c >= C) return;
-    float* p = cell_values + 4 * (size_t)c + 3;
-    if (alpha > 0.0f) *p = alpha * p_new[c] + (1.0f - alpha) * *p;
-    else *p = p_new[c];
+    p_update_body(C, p_new, cell_values, alpha, c);
+}
+
+}  // namespace wcfd
+
+// ---------------------------------------------------------------------------------
+// Batched forms: one launch for every case of a device case table; blockIdx.y is the
+// case, blockIdx.x runs over that case's faces or cells (blocks past the end of a smaller
+// case return at once).  The arithmetic is the single-case kernels' (same bodies).
+namespace wcfd {
+
+__global__ void __launch_bounds__(kBlock) face_pass_batched(const wcfd_case* __restrict__ cases, uint32_t mask,
+                                                            uint32_t flags) {
+    const wcfd_case& c = cases[blockIdx.y];
+    const int k = blockIdx.x * kBlock + threadIdx.x;
+    if (k >= c.mesh.n_faces) return;
+    face_pass_body(c.mesh, c.bc, c.state, mask, flags | (c.prm.skew ? 4u : 0u), k);
+}
+
+// mode 0: gradients only; 1: + divergence into case.div; 2: + velocity correction
+__global__ void __launch_bounds__(kBlock) gradient_batched(const wcfd_case* __restrict__ cases, uint32_t mask,
+                                                           int mode) {
+    const wcfd_case& c = cases[blockIdx.y];
+    const int i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= c.mesh.n_cells) return;
+    const CorrectArgs corr{mode == 2 ? c.hbya : nullptr, c.rua};
+    gradient_body(c.mesh, c.state, mask, mode == 1 ? c.div : nullptr, corr, i);
+}
+
+__global__ void __launch_bounds__(kBlock) hbya_batched(const wcfd_case* __restrict__ cases) {
+    const wcfd_case& c = cases[blockIdx.y];
+    const int i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= c.mesh.n_cells) return;
+    hbya_body(c.mesh.n_cells, c.state.cell_gradients, c.rua, c.hbya, c.state.cell_values, i);
+}
+
+__global__ void __launch_bounds__(kBlock) rua_faces_batched(const wcfd_case* __restrict__ cases) {
+    const wcfd_case& c = cases[blockIdx.y];
+    const int k = blockIdx.x * kBlock + threadIdx.x;
+    if (k >= c.mesh.n_faces) return;
+    cell_to_face_body(c.mesh, c.rua, c.rua_faces, k);
+}
+
+__global__ void __launch_bounds__(kBlock) p_update_batched(const wcfd_case* __restrict__ cases) {
+    const wcfd_case& c = cases[blockIdx.y];
+    const int i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= c.mesh.n_cells) return;
+    p_update_body(c.mesh.n_cells, c.p_x, c.state.cell_values, c.prm.steady ? c.prm.p_relax : 0.0f, i);
 }
 
 }  // namespace wcfd

@@ -23,6 +23,15 @@ __global__ void momentum_assemble_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s, 
 __global__ void pressure_assemble_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s, wcfd_system sys,
                                          const float* rua_faces, const float* div, wcfd_params prm);
 
+// batched forms over a device case table (blockIdx.y = case)
+__global__ void face_pass_batched(const wcfd_case* cases, uint32_t mask, uint32_t flags);
+__global__ void gradient_batched(const wcfd_case* cases, uint32_t mask, int mode);
+__global__ void hbya_batched(const wcfd_case* cases);
+__global__ void rua_faces_batched(const wcfd_case* cases);
+__global__ void p_update_batched(const wcfd_case* cases);
+__global__ void momentum_assemble_batched(const wcfd_case* cases);
+__global__ void pressure_assemble_batched(const wcfd_case* cases);
+
 // y = A x (NC = A.ncomp), launched from assemble.cu where the kernel template lives
 void launch_spmv(const wcfd_mesh& m, wcfd_system A, const float* x, float* y, cudaStream_t st);
 
@@ -41,6 +50,8 @@ struct KrylovArgs {
 const void* cg_kernel_for(int W);
 const void* bicgstab_kernel_for(int W);
 const void* cg_cluster_kernel_for(int W);
+const void* cg_cluster_batched_for(int W);
+const void* bicgstab_cluster_batched_for(int W);
 size_t cluster_cg_smem_bytes(int R, int W);
 
 inline int grid_for(long long n, int bs = kBlock) { return (int)((n + bs - 1) / bs); }

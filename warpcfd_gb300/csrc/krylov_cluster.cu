@@ -16,89 +16,19 @@
 //    neighbours (double-buffered p), so an iteration needs two barriers.
 // The arithmetic is that of cg_kernel (krylov.cu): the same Jacobi-preconditioned CG with
 // fp64 dot products and the same stop test.
+#include "cluster.cuh"
 #include "common.cuh"
 #include "kernels.cuh"
 
 namespace wcfd {
 
-constexpr int CBS = kClusterBlock;
-
-__device__ __forceinline__ unsigned cluster_rank() {
-    unsigned r;
-    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-    return r;
-}
-__device__ __forceinline__ unsigned cluster_nranks() {
-    unsigned r;
-    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
-    return r;
-}
-__device__ __forceinline__ void cluster_sync_all() {
-    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-// shared::cluster address of `p` (a pointer into this CTA's shared memory) in CTA `rank`
-__device__ __forceinline__ uint32_t map_rank(const void* p, unsigned rank) {
-    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
-    uint32_t r;
-    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
-    return r;
-}
-// Loads stay ordered against the cluster barrier (both are volatile asm) but carry no
-// memory clobber, so the compiler may keep several of them in flight.
-__device__ __forceinline__ float ld_cluster_f32(uint32_t addr) {
-    float v;
-    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(addr));
-    return v;
-}
-// value at packed column cp = (rank << 24) | local of an array laid out like `base` in
-// every CTA: a plain shared-memory load when this CTA owns it, a DSMEM load otherwise
-__device__ __forceinline__ float ld_col(const float* base, uint32_t cp, unsigned me) {
-    const unsigned rk = cp >> 24;
-    const uint32_t lo = cp & 0xFFFFFFu;
-    if (rk == me) return base[lo];
-    return ld_cluster_f32(map_rank(base + lo, rk));
-}
-__device__ __forceinline__ void st_cluster_v2f32(uint32_t addr, float a, float b) {
-    asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" :: "r"(addr), "f"(a), "f"(b) : "memory");
-}
-
-// All-reduce over the cluster of NV float-float accumulators: the CTA total is stored
-// into slot `me` of every CTA's shared memory, and after the barrier warp 0 of each CTA
-// merges the cs slots in a fixed order and one thread converts to fp64, so every CTA gets
-// the same bits.  Slots are double-buffered by `parity`.
-template <int NV>
-__device__ __forceinline__ void cluster_allreduce(ff (&acc)[NV], double (&out)[NV], ff* slots, unsigned parity,
-                                                  unsigned me, unsigned cs) {
-    __shared__ double res[NV];
-    block_reduce_ff<NV, CBS>(acc);
-    ff* base = slots + parity * (NV * 16);
-    if (threadIdx.x < cs) {
-#pragma unroll
-        for (int i = 0; i < NV; ++i)
-            st_cluster_v2f32(map_rank(base + i * 16 + me, threadIdx.x), acc[i].hi, acc[i].lo);
-    }
-    cluster_sync_all();
-    if (threadIdx.x < 32) {
-        const unsigned lane = threadIdx.x;
-#pragma unroll
-        for (int i = 0; i < NV; ++i) {
-            ff x = lane < cs ? base[i * 16 + lane] : ff_zero();
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) ff_shfl_merge(x, o);
-            if (lane == 0) res[i] = ff_to_double(x);
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < NV; ++i) out[i] = res[i];
-}
-
 // dynamic shared memory per CTA for R rows and width W:
-// off + packed columns (8 W) and diag, invd, x, r, p (two buffers), q (28)
-size_t cluster_cg_smem_bytes(int R, int W) { return (size_t)R * (8 * (size_t)W + 28); }
+// off + packed columns (8 W) and diag, invd, r, p (two buffers), q (24); x stays in global
+// memory (own rows only, coalesced) so 16 CTAs hold 65536 rows of width 4
+size_t cluster_cg_smem_bytes(int R, int W) { return (size_t)R * (8 * (size_t)W + 24); }
 
 template <int W>
-__global__ void __launch_bounds__(CBS) cg_cluster_kernel(KrylovArgs a, int R) {
+__device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ ff slots[2 * 2 * 16];
     struct Scal {
@@ -116,8 +46,8 @@ __global__ void __launch_bounds__(CBS) cg_cluster_kernel(KrylovArgs a, int R) {
     uint32_t* colp = reinterpret_cast<uint32_t*>(off + (size_t)W * R);  // [W][R] (rank << 24) | local
     float* diag = reinterpret_cast<float*>(colp + (size_t)W * R);
     float* invd = diag + R;
-    float* x = invd + R;
-    float* r = x + R;
+    float* r = invd + R;
+    float* x = a.x + row0;  // global, own rows
     float* pbuf0 = r + R;
     float* pbuf1 = pbuf0 + R;
     float* q = pbuf1 + R;
@@ -127,7 +57,6 @@ __global__ void __launch_bounds__(CBS) cg_cluster_kernel(KrylovArgs a, int R) {
         const int g = row0 + l;
         diag[l] = a.A.diag[g];
         invd[l] = diag[l] != 0.0f ? 1.0f / diag[l] : 1.0f;
-        x[l] = a.x[g];
 #pragma unroll
         for (int j = 0; j < W; ++j) {
             off[(size_t)j * R + l] = a.A.off[(size_t)j * C + g];
@@ -142,7 +71,7 @@ __global__ void __launch_bounds__(CBS) cg_cluster_kernel(KrylovArgs a, int R) {
     for (int l = threadIdx.x; l < nloc; l += CBS) {
         float ax = diag[l] * x[l];
 #pragma unroll
-        for (int j = 0; j < W; ++j) ax += off[(size_t)j * R + l] * ld_col(x, colp[(size_t)j * R + l], me);
+        for (int j = 0; j < W; ++j) ax += off[(size_t)j * R + l] * a.x[a.m.ell_col[(size_t)j * C + row0 + l]];
         const float ri = a.A.rhs[row0 + l] - ax;
         const float zi = ri * invd[l];
         r[l] = ri;
@@ -221,7 +150,6 @@ __global__ void __launch_bounds__(CBS) cg_cluster_kernel(KrylovArgs a, int R) {
         __syncthreads();
         cur ^= 1;
     }
-    for (int l = threadIdx.x; l < nloc; l += CBS) a.x[row0 + l] = x[l];
     if (me == 0 && threadIdx.x == 0) {
         int st = sc.status;
         if (st == WCFD_OK && !(sc.rr <= a.atol2)) st = WCFD_NOT_CONVERGED;
@@ -230,6 +158,244 @@ __global__ void __launch_bounds__(CBS) cg_cluster_kernel(KrylovArgs a, int R) {
         a.stats->residual = sqrt(sc.rr);
     }
 }
+
+template <int W>
+__global__ void __launch_bounds__(CBS) cg_cluster_kernel(KrylovArgs a, int R) {
+    cg_cluster_body<W>(a, R);
+}
+
+// One cluster per case of a device case table: the pressure CG of every case
+// (pres system, p_x warm start, stats[1]), cs CTAs per cluster.
+template <int W>
+__global__ void __launch_bounds__(CBS) cg_cluster_batched(const wcfd_case* __restrict__ cases, int cs) {
+    const wcfd_case& c = cases[blockIdx.x / cs];
+    KrylovArgs a = {};
+    a.m = c.mesh;
+    a.A = c.pres;
+    a.x = c.p_x;
+    a.atol2 = c.prm.atol_p * c.prm.atol_p;
+    a.maxiter = c.prm.maxiter;
+    a.stats = c.stats + 1;
+    cg_cluster_body<W>(a, (c.mesh.n_cells + cs - 1) / cs);
+}
+
+// BiCGSTAB on one case per cluster, for the batched form: the momentum system of the
+// case (interleaved 3C rows, shared off-diagonals) with its vectors in global memory
+// (the case's workspace: r, r0, pA, pB, vA, vB, t, s, invd), rows spread over the cluster's
+// CTAs, hardware cluster barriers and the DSMEM all-reduce.  Values written by another CTA
+// during the solve are read through L2 (ld.cg).  Same algorithm and arithmetic as
+// bicgstab_kernel (krylov.cu).
+template <int W>
+__global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case* __restrict__ cases, int cs_req) {
+    __shared__ ff slots[2 * 2 * 16];
+    struct Scal {
+        double rr, rho, alpha;
+        float af, bf, of;
+        int go, status, k;
+    };
+    __shared__ Scal sc;
+    const wcfd_case& cse = cases[blockIdx.x / cs_req];
+    const unsigned me = cluster_rank();
+    const unsigned cs = cluster_nranks();
+    const int C = cse.mesh.n_cells;
+    const size_t n3 = 3 * (size_t)C;
+    float* ws = cse.ws_u.vec;
+    float* r = ws;
+    float* r0 = ws + n3;
+    float* pbuf[2] = {ws + 2 * n3, ws + 3 * n3};
+    float* vbuf[2] = {ws + 4 * n3, ws + 5 * n3};
+    float* t = ws + 6 * n3;
+    float* s = ws + 7 * n3;
+    float* invd = ws + 8 * n3;
+    const float* __restrict__ b = cse.mom.rhs;
+    const float* __restrict__ diag = cse.mom.diag;
+    const float* __restrict__ off = cse.mom.off;
+    const int* __restrict__ col = cse.mesh.ell_col;
+    float* x = cse.hbya;
+    const double atol2 = cse.prm.atol_u * cse.prm.atol_u;
+    const int maxiter = cse.prm.maxiter;
+    const int stride = (int)cs * CBS;
+    const int i0 = (int)me * CBS + threadIdx.x;
+    unsigned parity = 0;
+
+    ff acc[1] = {ff_zero()};
+    for (int i = i0; i < C; i += stride) {
+        float ax[3];
+#pragma unroll
+        for (int o = 0; o < 3; ++o) ax[o] = diag[3 * (size_t)i + o] * x[3 * (size_t)i + o];
+#pragma unroll
+        for (int j = 0; j < W; ++j) {
+            const float v = off[(size_t)j * C + i];
+            const int c = col[(size_t)j * C + i];
+#pragma unroll
+            for (int o = 0; o < 3; ++o) ax[o] += v * x[3 * (size_t)c + o];
+        }
+#pragma unroll
+        for (int o = 0; o < 3; ++o) {
+            const size_t q = 3 * (size_t)i + o;
+            const float ri = b[q] - ax[o];
+            r[q] = ri;
+            r0[q] = ri;
+            pbuf[0][q] = ri;
+            vbuf[0][q] = 0.0f;
+            invd[q] = diag[q] != 0.0f ? 1.0f / diag[q] : 1.0f;
+            ff_fma(acc[0], ri, ri);
+        }
+    }
+    double red[1];
+    cluster_allreduce<1>(acc, red, slots, parity, me, cs);
+    parity ^= 1u;
+    if (threadIdx.x == 0) {
+        sc.rr = red[0];
+        sc.rho = red[0];
+        sc.bf = 0.0f;
+        sc.of = 0.0f;
+        sc.k = 0;
+        sc.status = WCFD_OK;
+        sc.go = (0 < maxiter && red[0] > atol2);
+    }
+    __syncthreads();
+    int cur = 0;
+    while (sc.go) {
+        const float bf = sc.bf, of0 = sc.of;
+        const float* po = pbuf[cur];
+        const float* vo = vbuf[cur];
+        float* pn = pbuf[cur ^ 1];
+        float* vn = vbuf[cur ^ 1];
+        ff accv[1] = {ff_zero()};
+        for (int i = i0; i < C; i += stride) {
+            float pi[3], vi[3];
+#pragma unroll
+            for (int o = 0; o < 3; ++o) {
+                const size_t q = 3 * (size_t)i + o;
+                pi[o] = __ldcg(r + q) + bf * (__ldcg(po + q) - of0 * __ldcg(vo + q));
+                vi[o] = diag[q] * (pi[o] * __ldcg(invd + q));
+            }
+#pragma unroll
+            for (int j = 0; j < W; ++j) {
+                const float v = off[(size_t)j * C + i];
+                const int c = col[(size_t)j * C + i];
+#pragma unroll
+                for (int o = 0; o < 3; ++o) {
+                    const size_t q = 3 * (size_t)c + o;
+                    const float pc = __ldcg(r + q) + bf * (__ldcg(po + q) - of0 * __ldcg(vo + q));
+                    vi[o] += v * (pc * __ldcg(invd + q));
+                }
+            }
+#pragma unroll
+            for (int o = 0; o < 3; ++o) {
+                const size_t q = 3 * (size_t)i + o;
+                pn[q] = pi[o];
+                vn[q] = vi[o];
+                ff_fma(accv[0], r0[q], vi[o]);
+            }
+        }
+        double r0v[1];
+        cluster_allreduce<1>(accv, r0v, slots, parity, me, cs);
+        parity ^= 1u;
+        if (threadIdx.x == 0) {
+            if (r0v[0] == 0.0) {
+                sc.status = WCFD_KRYLOV_BREAKDOWN;
+                sc.go = 0;
+            } else {
+                sc.alpha = sc.rho / r0v[0];
+                sc.af = (float)sc.alpha;
+            }
+        }
+        __syncthreads();
+        if (!sc.go) break;
+        const float af = sc.af;
+        ff acct[2] = {ff_zero(), ff_zero()};
+        for (int i = i0; i < C; i += stride) {
+            float si[3], ti[3];
+#pragma unroll
+            for (int o = 0; o < 3; ++o) {
+                const size_t q = 3 * (size_t)i + o;
+                si[o] = __ldcg(r + q) - af * __ldcg(vn + q);
+                x[q] += af * (pn[q] * invd[q]);
+                ti[o] = diag[q] * (si[o] * invd[q]);
+            }
+#pragma unroll
+            for (int j = 0; j < W; ++j) {
+                const float v = off[(size_t)j * C + i];
+                const int c = col[(size_t)j * C + i];
+#pragma unroll
+                for (int o = 0; o < 3; ++o) {
+                    const size_t q = 3 * (size_t)c + o;
+                    const float scv = __ldcg(r + q) - af * __ldcg(vn + q);
+                    ti[o] += v * (scv * __ldcg(invd + q));
+                }
+            }
+#pragma unroll
+            for (int o = 0; o < 3; ++o) {
+                const size_t q = 3 * (size_t)i + o;
+                s[q] = si[o];
+                t[q] = ti[o];
+                ff_fma(acct[0], ti[o], ti[o]);
+                ff_fma(acct[1], ti[o], si[o]);
+            }
+        }
+        double ts[2];
+        cluster_allreduce<2>(acct, ts, slots, parity, me, cs);
+        parity ^= 1u;
+        if (threadIdx.x == 0) sc.of = (float)(ts[0] != 0.0 ? ts[1] / ts[0] : 0.0);
+        __syncthreads();
+        const float of = sc.of;
+        ff accr[2] = {ff_zero(), ff_zero()};
+        for (int i = i0; i < C; i += stride) {
+#pragma unroll
+            for (int o = 0; o < 3; ++o) {
+                const size_t q = 3 * (size_t)i + o;
+                const float si = s[q];
+                x[q] += of * (si * invd[q]);
+                const float ri = si - of * t[q];
+                r[q] = ri;
+                ff_fma(accr[0], ri, ri);
+                ff_fma(accr[1], r0[q], ri);
+            }
+        }
+        double rr2[2];
+        cluster_allreduce<2>(accr, rr2, slots, parity, me, cs);
+        parity ^= 1u;
+        if (threadIdx.x == 0) {
+            const double omega = ts[0] != 0.0 ? ts[1] / ts[0] : 0.0;
+            sc.rr = rr2[0];
+            sc.k += 1;
+            if (omega == 0.0 || sc.rho == 0.0) {
+                sc.status = WCFD_KRYLOV_BREAKDOWN;
+                sc.go = 0;
+            } else {
+                sc.bf = (float)((rr2[1] / sc.rho) * (sc.alpha / omega));
+                sc.rho = rr2[1];
+                sc.go = (sc.k < maxiter && sc.rr > atol2);
+            }
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+    if (me == 0 && threadIdx.x == 0) {
+        int st = sc.status;
+        if (st == WCFD_OK && !(sc.rr <= atol2)) st = WCFD_NOT_CONVERGED;
+        cse.stats[0].iterations = sc.k;
+        cse.stats[0].status = st;
+        cse.stats[0].residual = sqrt(sc.rr);
+    }
+}
+
+#define WCFD_W_SWITCH(NAME)                      \
+    switch (W) {                                 \
+        case 0: return (const void*)NAME<0>;     \
+        case 1: return (const void*)NAME<1>;     \
+        case 2: return (const void*)NAME<2>;     \
+        case 3: return (const void*)NAME<3>;     \
+        case 4: return (const void*)NAME<4>;     \
+        case 5: return (const void*)NAME<5>;     \
+        case 6: return (const void*)NAME<6>;     \
+        default: return nullptr;                 \
+    }
+
+const void* cg_cluster_batched_for(int W) { WCFD_W_SWITCH(cg_cluster_batched) }
+const void* bicgstab_cluster_batched_for(int W) { WCFD_W_SWITCH(bicgstab_cluster_batched) }
 
 const void* cg_cluster_kernel_for(int W) {
     switch (W) {
