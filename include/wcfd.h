@@ -111,8 +111,10 @@ typedef struct wcfd_krylov_ws {
 
 typedef struct wcfd_solve_stats {
     int32_t iterations;
-    int32_t status;       /* WCFD_OK, WCFD_NOT_CONVERGED, WCFD_KRYLOV_BREAKDOWN, WCFD_BARRIER_TIMEOUT */
-    double  residual;     /* ||b - A x||_2 at exit (fp64)                         */
+    int32_t status;            /* WCFD_OK, WCFD_NOT_CONVERGED, WCFD_KRYLOV_BREAKDOWN, WCFD_BARRIER_TIMEOUT */
+    double  residual;          /* ||b - A x||_2 at exit (fp64)                              */
+    double  initial_residual;  /* ||b - A x0||_2 at entry: the outer iteration's residual   */
+    double  rhs_norm;          /* ||b||_2                                                   */
 } wcfd_solve_stats;
 
 /* per-case scalars of one SIMPLE iteration / PISO step */

@@ -1,0 +1,75 @@
+"""Batched form: each case gives the same result alone and in the mix.
+
+* in the mix vs alone in a batch of one with the same cluster size: bitwise equal (every
+  case's kernels and its cluster's reductions do not depend on the other cases);
+* in the mix vs the single-case drop-in path (grid/cluster Krylov kernels with their own
+  partition): within the step-parity tolerances of test_gpu_parity.py, with the same
+  Krylov iteration counts (+-2).
+"""
+import numpy as np
+import pytest
+import torch
+
+from tests.cases import cavity3d_bc, cavity3d_mesh, cavity_bc, cavity_mesh, channel_bc, channel_mesh
+from tests.gpu_helpers import fields, make_pair, rel_l2, vel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib_ready():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from warpcfd_gb300.build import build_library
+    build_library()
+
+
+def _cases():
+    specs = [(lambda: cavity_mesh(16), cavity_bc, 0, 0.01),
+             (lambda: cavity_mesh(24, jitter=0.1, seed=2), cavity_bc, 0, 0.005),
+             (lambda: channel_mesh(40, 8), channel_bc, None, 0.05),
+             (lambda: cavity_mesh(32), cavity_bc, 0, 0.002)]
+    out = []
+    for mk, bc, ref, nu in specs:
+        model, solver, _ = make_pair(mk(), bc, ref_cell=ref, nu=nu)
+        out.append((model, solver))
+    return out
+
+
+def test_mix_equals_alone_and_drop_in():
+    from warpcfd_gb300.batch import CaseBatch
+
+    steps = 5
+    mix = _cases()
+    batch = CaseBatch([s for _, s in mix])
+    cs = batch.cluster_size
+    assert cs >= 1
+    for _ in range(steps):
+        batch.step()
+    got = [fields(m) for m, _ in mix]
+    st_mix = batch.solve_stats()
+    for i, (mk_model, mk_solver) in enumerate(_cases()):
+        alone = CaseBatch([mk_solver], cluster_size=cs)
+        for _ in range(steps):
+            alone.step()
+        assert np.array_equal(fields(mk_model), got[i]), i
+    for i, (model, solver) in enumerate(_cases()):
+        for _ in range(steps):
+            solver.step()
+        ref = fields(model)
+        for o in range(3):
+            assert vel_err(got[i], ref, o) < 1e-4, (i, o)
+        assert rel_l2(got[i][:, 3], ref[:, 3]) < 1e-3, i
+        st = solver.solve_stats()
+        assert abs(st[1]["iterations"] - int(st_mix[i, 1]["iterations"])) <= 2, i
+    res = batch.relative_residuals()
+    assert np.all(np.isfinite(res)) and np.all(res > 0)
+
+
+def test_batch_rejects_mixed_widths():
+    from warpcfd_gb300.batch import CaseBatch
+
+    m2, s2, _ = make_pair(cavity_mesh(8), cavity_bc)
+    m3, s3, _ = make_pair(cavity3d_mesh(4), cavity3d_bc)
+    with pytest.raises(ValueError):
+        CaseBatch([s2, s3])

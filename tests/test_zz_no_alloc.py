@@ -23,8 +23,10 @@ MAX_CELLS = 131072   # WCFD_NOALLOC_MAX_CELLS in include/wcfd.h
 
 
 def _stats(t):
-    raw = np.frombuffer(t.cpu().numpy().tobytes(), dtype=np.dtype([("it", "<i4"), ("st", "<i4"), ("res", "<f8")]))
-    return int(raw["it"][0]), int(raw["st"][0]), float(raw["res"][0])
+    from warpcfd_gb300 import _lib
+
+    raw = np.frombuffer(t.cpu().numpy().tobytes(), dtype=_lib.STATS_DTYPE)
+    return int(raw["iterations"][0]), int(raw["status"][0]), float(raw["residual"][0])
 
 
 def test_noalloc_cg_matches_workspace_cg():
@@ -50,7 +52,7 @@ def test_noalloc_cg_matches_workspace_cg():
     C = model.num_cells
 
     x_ref = torch.zeros(C, dtype=torch.float32, device="cuda")
-    st_ref = torch.zeros(16, dtype=torch.uint8, device="cuda")
+    st_ref = torch.zeros(_lib.STATS_BYTES, dtype=torch.uint8, device="cuda")
     # the reference result comes from wcfd_cg on its grid-cooperative kernel, the one the
     # allocation-free entry point runs, so the two must agree to the last bit
     assert lib.wcfd_set_krylov_path(1) == 0
@@ -66,7 +68,7 @@ def test_noalloc_cg_matches_workspace_cg():
 
     for _ in range(2):
         x = torch.zeros(C, dtype=torch.float32, device="cuda")
-        st = torch.zeros(16, dtype=torch.uint8, device="cuda")
+        st = torch.zeros(_lib.STATS_BYTES, dtype=torch.uint8, device="cuda")
         rc = fn(ct.byref(mesh_t), pe.system_struct(), ct.c_void_p(x.data_ptr()), 1e-6, 500,
                 ct.c_void_p(st.data_ptr()), stream)
         assert rc == 0, lib.wcfd_last_error()

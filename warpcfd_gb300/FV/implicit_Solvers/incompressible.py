@@ -17,7 +17,7 @@ from ... import _lib
 from ..model import FVM, _stream
 from ..terms import ConvectionTerm, DdtTerm, DiffusionTerm, Equation, GradTerm
 
-STATS_DTYPE = np.dtype([("iterations", "<i4"), ("status", "<i4"), ("residual", "<f8")])
+STATS_DTYPE = _lib.STATS_DTYPE
 
 
 class IncompressibleSolver:
@@ -140,7 +140,8 @@ class IncompressibleSolver:
         """(momentum, pressure) Krylov outcomes of the last step: iterations, status, residual."""
         raw = np.frombuffer(self.stats.cpu().numpy().tobytes(), dtype=STATS_DTYPE)
         return [dict(iterations=int(r["iterations"]), status=_lib.STATUS_NAMES.get(int(r["status"]), "?"),
-                     residual=float(r["residual"])) for r in raw]
+                     residual=float(r["residual"]), initial_residual=float(r["initial_residual"]),
+                     rhs_norm=float(r["rhs_norm"])) for r in raw]
 
     def momentum_residual_operator(self):
         return self.vel_equation.apply

@@ -61,7 +61,7 @@ class Equation:
         self.ws_partials = torch.zeros(8 * _lib.MAX_BLOCKS, dtype=torch.float64, device=dev)
         self.ws_results = torch.zeros(8, dtype=torch.float64, device=dev)
         self.ws_barrier = torch.zeros(_lib.BARRIER_WORDS, dtype=torch.int32, device=dev)
-        self.stats = torch.zeros(16, dtype=torch.uint8, device=dev)
+        self.stats = torch.zeros(_lib.STATS_BYTES, dtype=torch.uint8, device=dev)
 
     @property
     def x(self):
@@ -132,7 +132,7 @@ class Equation:
         _lib.call(fn, ct.byref(m), self.system_struct(), ct.c_void_p(x.data_ptr()), self.workspace_struct(),
                   float(self.tol), int(self.max_iter), ct.c_void_p(self.stats.data_ptr()),
                   ct.c_void_p(torch.cuda.current_stream().cuda_stream))
-        raw = np.frombuffer(self.stats.cpu().numpy().tobytes(),
-                            dtype=np.dtype([("iterations", "<i4"), ("status", "<i4"), ("residual", "<f8")]))[0]
+        raw = np.frombuffer(self.stats.cpu().numpy().tobytes(), dtype=_lib.STATS_DTYPE)[0]
         return dict(iterations=int(raw["iterations"]), status=_lib.STATUS_NAMES.get(int(raw["status"]), "?"),
-                    residual=float(raw["residual"])), x
+                    residual=float(raw["residual"]), initial_residual=float(raw["initial_residual"]),
+                    rhs_norm=float(raw["rhs_norm"])), x

@@ -25,6 +25,14 @@ STATUS_NAMES = {0: "ok", 1: "bad argument", 2: "cuda error", 3: "krylov breakdow
 WCFD_U, WCFD_V, WCFD_W, WCFD_P, WCFD_ALL = 1, 2, 4, 8, 15
 MAX_BLOCKS = 2048
 BARRIER_WORDS = MAX_BLOCKS + 4
+STATS_BYTES = 32
+
+try:  # numpy view of wcfd_solve_stats
+    import numpy as _np
+    STATS_DTYPE = _np.dtype([("iterations", "<i4"), ("status", "<i4"), ("residual", "<f8"),
+                             ("initial_residual", "<f8"), ("rhs_norm", "<f8")])
+except ImportError:  # pragma: no cover
+    STATS_DTYPE = None
 
 vp = ct.c_void_p
 
@@ -55,7 +63,8 @@ class KrylovWS_t(ct.Structure):
 
 
 class Stats_t(ct.Structure):
-    _fields_ = [("iterations", ct.c_int32), ("status", ct.c_int32), ("residual", ct.c_double)]
+    _fields_ = [("iterations", ct.c_int32), ("status", ct.c_int32), ("residual", ct.c_double),
+                ("initial_residual", ct.c_double), ("rhs_norm", ct.c_double)]
 
 
 class Params_t(ct.Structure):

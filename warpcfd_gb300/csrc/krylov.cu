@@ -27,7 +27,7 @@ __device__ __forceinline__ float jacobi(float d) { return d != 0.0f ? 1.0f / d :
 
 // Krylov scalars of one block, owned by thread 0
 struct KScalars {
-    double rr, rz, rho, alpha;
+    double rr, rz, rho, alpha, rr0, bb;
     float af, bf, of;
     int go, status, k;
 };
@@ -60,6 +60,8 @@ __device__ void write_stats(const KrylovArgs& a, const KScalars& sc) {
         a.stats->iterations = sc.k;
         a.stats->status = st;
         a.stats->residual = sqrt(sc.rr);
+        a.stats->initial_residual = sqrt(sc.rr0);
+        a.stats->rhs_norm = sqrt(sc.bb);
     }
 }
 
@@ -87,8 +89,8 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
         sc.status = WCFD_OK;
     }
 
-    // r = b - A x ; z = M r ; p = z ; rr = r.r ; rz = r.z
-    ff acc[2] = {ff_zero(), ff_zero()};
+    // r = b - A x ; z = M r ; p = z ; rr = r.r ; rz = r.z ; bb = b.b
+    ff acc[3] = {ff_zero(), ff_zero(), ff_zero()};
     for (int i = i0; i < C; i += stride) {
         float ax = diag[i] * x[i];
 #pragma unroll
@@ -101,11 +103,14 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
         pbuf[0][i] = zi;
         ff_fma(acc[0], ri, ri);
         ff_fma(acc[1], ri, zi);
+        ff_fma(acc[2], b[i], b[i]);
     }
-    double red[2];
-    SYNC(2, acc, red);
+    double red[3];
+    SYNC(3, acc, red);
     if (threadIdx.x == 0) {
         sc.rr = red[0];
+        sc.rr0 = red[0];
+        sc.bb = red[2];
         sc.rz = red[1];
         sc.bf = 0.0f;  // the first direction is z itself
         sc.go = (0 < a.maxiter && red[0] > a.atol2);
@@ -196,8 +201,8 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
         sc.status = WCFD_OK;
     }
 
-    // r = b - A x ; r0 = r ; p = r ; v = 0 ; rr ; rho = r0.r = rr
-    ff acc[1] = {ff_zero()};
+    // r = b - A x ; r0 = r ; p = r ; v = 0 ; rr ; rho = r0.r = rr ; bb = b.b
+    ff acc[2] = {ff_zero(), ff_zero()};
     for (int i = i0; i < C; i += stride) {
         float ax[3];
 #pragma unroll
@@ -219,12 +224,15 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
             vbuf[0][q] = 0.0f;
             invd[q] = jacobi(diag[q]);
             ff_fma(acc[0], ri, ri);
+            ff_fma(acc[1], b[q], b[q]);
         }
     }
-    double red[1];
-    SYNC(1, acc, red);
+    double red[2];
+    SYNC(2, acc, red);
     if (threadIdx.x == 0) {
         sc.rr = red[0];
+        sc.rr0 = red[0];
+        sc.bb = red[1];
         sc.rho = red[0];
         sc.bf = 0.0f;  // the first direction is r itself
         sc.of = 0.0f;

@@ -30,9 +30,9 @@ size_t cluster_cg_smem_bytes(int R, int W) { return (size_t)R * (8 * (size_t)W +
 template <int W>
 __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ ff slots[2 * 2 * 16];
+    __shared__ ff slots[2 * 3 * 16];
     struct Scal {
-        double rr, rz;
+        double rr, rz, rr0, bb;
         float af, bf;
         int go, status, k;
     };
@@ -66,8 +66,8 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
         }
     }
     cluster_sync_all();
-    // r = b - A x ; p = z = M r ; rr ; rz
-    ff acc[2] = {ff_zero(), ff_zero()};
+    // r = b - A x ; p = z = M r ; rr ; rz ; bb
+    ff acc[3] = {ff_zero(), ff_zero(), ff_zero()};
     for (int l = threadIdx.x; l < nloc; l += CBS) {
         float ax = diag[l] * x[l];
 #pragma unroll
@@ -78,14 +78,17 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
         pbuf0[l] = zi;
         ff_fma(acc[0], ri, ri);
         ff_fma(acc[1], ri, zi);
+        ff_fma(acc[2], a.A.rhs[row0 + l], a.A.rhs[row0 + l]);
     }
     unsigned parity = 0;
-    double red[2];
-    cluster_allreduce<2>(acc, red, slots, parity, me, cs);
+    double red[3];
+    cluster_allreduce<3>(acc, red, slots, parity, me, cs);
     parity ^= 1u;
     // fp64 scalar work by thread 0 only (fp64 runs at ~1/64 of the fp32 rate on GB300)
     if (threadIdx.x == 0) {
         sc.rr = red[0];
+        sc.rr0 = red[0];
+        sc.bb = red[2];
         sc.rz = red[1];
         sc.bf = 0.0f;
         sc.k = 0;
@@ -156,6 +159,8 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
         a.stats->iterations = sc.k;
         a.stats->status = st;
         a.stats->residual = sqrt(sc.rr);
+        a.stats->initial_residual = sqrt(sc.rr0);
+        a.stats->rhs_norm = sqrt(sc.bb);
     }
 }
 
@@ -187,9 +192,9 @@ __global__ void __launch_bounds__(CBS) cg_cluster_batched(const wcfd_case* __res
 // bicgstab_kernel (krylov.cu).
 template <int W>
 __global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case* __restrict__ cases, int cs_req) {
-    __shared__ ff slots[2 * 2 * 16];
+    __shared__ ff slots[2 * 3 * 16];
     struct Scal {
-        double rr, rho, alpha;
+        double rr, rho, alpha, rr0, bb;
         float af, bf, of;
         int go, status, k;
     };
@@ -218,7 +223,7 @@ __global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case*
     const int i0 = (int)me * CBS + threadIdx.x;
     unsigned parity = 0;
 
-    ff acc[1] = {ff_zero()};
+    ff acc[2] = {ff_zero(), ff_zero()};
     for (int i = i0; i < C; i += stride) {
         float ax[3];
 #pragma unroll
@@ -240,13 +245,16 @@ __global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case*
             vbuf[0][q] = 0.0f;
             invd[q] = diag[q] != 0.0f ? 1.0f / diag[q] : 1.0f;
             ff_fma(acc[0], ri, ri);
+            ff_fma(acc[1], b[q], b[q]);
         }
     }
-    double red[1];
-    cluster_allreduce<1>(acc, red, slots, parity, me, cs);
+    double red[2];
+    cluster_allreduce<2>(acc, red, slots, parity, me, cs);
     parity ^= 1u;
     if (threadIdx.x == 0) {
         sc.rr = red[0];
+        sc.rr0 = red[0];
+        sc.bb = red[1];
         sc.rho = red[0];
         sc.bf = 0.0f;
         sc.of = 0.0f;
@@ -379,6 +387,8 @@ __global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case*
         cse.stats[0].iterations = sc.k;
         cse.stats[0].status = st;
         cse.stats[0].residual = sqrt(sc.rr);
+        cse.stats[0].initial_residual = sqrt(sc.rr0);
+        cse.stats[0].rhs_norm = sqrt(sc.bb);
     }
 }
 
