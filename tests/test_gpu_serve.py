@@ -1,0 +1,37 @@
+"""Serving loop: continuous batching over a small seeded request mix.
+
+Every request completes; each result (iterations and fields) is the same when the request
+is served alone as when it is served in the mix (bitwise: each case's kernels and cluster
+reductions do not depend on the other cases of its bucket, and the bucket's cluster size
+is fixed by its bound).
+"""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib_ready():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from warpcfd_gb300.build import build_library
+    build_library()
+
+
+def test_served_alone_equals_in_mix():
+    from warpcfd_gb300.serve import Server, make_request_mix
+
+    reqs = make_request_mix(10, seed=7, rate=400.0, lo=32 * 32, hi=64 * 64)
+    kw = dict(tol=1e-4, check_every=10, max_outer=300, buckets=(1024, 4096), keep_fields=True, atol=1e-7)
+    mix = Server(**kw).run(reqs)
+    assert len(mix.results) == len(reqs)
+    s = mix.summary()
+    assert s["max_active"] > 1 and s["p99_s"] >= s["p50_s"] > 0
+    by_id = {r.rid: r for r in mix.results}
+    for req in reqs[:4]:
+        alone = Server(**kw).run([req]).results[0]
+        got = by_id[req.rid]
+        assert alone.iterations == got.iterations
+        assert torch.equal(alone.fields, got.fields)

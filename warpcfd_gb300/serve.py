@@ -1,0 +1,313 @@
+"""Continuous-batching server for steady incompressible cases.
+
+Requests arrive over time (seeded Poisson arrivals).  Each is a lid-driven cavity or a
+channel of its own size, Reynolds number and lid/inlet speed.  The server
+
+* admits a waiting request when its arrival time has passed, a batch slot is free and the
+  HBM budget (the measured device bytes of the admitted cases) has room for its estimate;
+* keeps every admitted case's fields, geometry and systems resident on the device;
+* advances all admitted cases together with the batched form (``CaseBatch``): one launch
+  sequence per outer iteration per size bucket, buckets on separate streams so their work
+  overlaps on the device;
+* every ``check_every`` iterations reads all cases' residuals with one copy per bucket,
+  retires the converged ones (relative momentum residual below ``tol``) and admits new
+  requests into the freed slots;
+* records time-to-converged-solution (completion - arrival) per request and the
+  cell-iterations done.
+
+Mesh sizes are quantised to a log-spaced ladder of side lengths (about 8% apart) so
+preprocessed meshes are cached and reused across requests.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from .batch import CaseBatch
+from .FV import FVM
+from .FV.implicit_Solvers import IncompressibleSolver
+from .preprocess import Mesh, create_2D_grid, define_boundary_walls
+
+CHANNEL_ASPECT = 4  # channel cases: (4 n) x n cells on a 4 x 1 domain
+
+
+@dataclass
+class Request:
+    rid: int
+    kind: str          # "cavity" or "channel"
+    cells: int         # requested cell count
+    re: float
+    speed: float
+    arrival: float     # seconds after the start of the run
+
+
+@dataclass
+class Result:
+    rid: int
+    kind: str
+    cells: int
+    iterations: int
+    converged: bool
+    residual: float
+    arrival: float
+    admitted: float
+    finished: float
+    fields: object = None
+
+    @property
+    def latency(self):
+        return self.finished - self.arrival
+
+
+def side_ladder(lo=32, hi=256, steps=28):
+    """Log-spaced cavity side lengths (cells) from lo to hi."""
+    return sorted({int(round(lo * (hi / lo) ** (i / (steps - 1)))) for i in range(steps)})
+
+
+def make_request_mix(n_requests=1024, seed=0, rate=200.0, lo=32 * 32, hi=256 * 256):
+    """Seeded mix: cells log-uniform in [lo, hi], Re ~ U[50, 1000], speed ~ U[0.5, 2],
+    cavity or channel with a fair coin, Poisson arrivals at ``rate`` per second."""
+    rng = np.random.default_rng(seed)
+    cells = np.exp(rng.uniform(np.log(lo), np.log(hi), n_requests)).astype(np.int64)
+    re = rng.uniform(50.0, 1000.0, n_requests)
+    speed = rng.uniform(0.5, 2.0, n_requests)
+    kind = np.where(rng.random(n_requests) < 0.5, "cavity", "channel")
+    arrival = np.cumsum(rng.exponential(1.0 / rate, n_requests))
+    return [Request(i, str(kind[i]), int(cells[i]), float(re[i]), float(speed[i]), float(arrival[i]))
+            for i in range(n_requests)]
+
+
+class MeshCache:
+    def __init__(self):
+        self.ladder = side_ladder()
+        self.meshes = {}
+
+    def shape(self, kind, cells):
+        if kind == "cavity":
+            n = min(self.ladder, key=lambda s: abs(math.log(s * s / cells)))
+            return (n, n)
+        ny = min(self.ladder, key=lambda s: abs(math.log(CHANNEL_ASPECT * s * s / cells)))
+        return (CHANNEL_ASPECT * ny, ny)
+
+    def get(self, kind, cells):
+        nx, ny = self.shape(kind, cells)
+        key = (kind, nx, ny)
+        if key not in self.meshes:
+            lx = 1.0 if kind == "cavity" else float(CHANNEL_ASPECT)
+            m = Mesh(create_2D_grid((0, 0, 0), nx, ny, lx, 1.0, 0.1))
+            define_boundary_walls(m)
+            self.meshes[key] = m
+        return self.meshes[key]
+
+
+def build_solver(req: Request, mesh, atol=1e-8, maxiter=500, device=None):
+    """FVM + SIMPLE solver of one request (relaxation 0.7 / 0.3, nu = speed * L / Re)."""
+    nu = req.speed * 1.0 / req.re
+    model = FVM(mesh, device=device)
+    model.material.create_incompressible_newtonian_fluid(viscosity=nu, density=1.0)
+    b = model.boundary
+    if req.kind == "cavity":
+        model.set_reference_pressure(0, 0.0)
+        b.no_slip_wall("-X")
+        b.no_slip_wall("+X")
+        b.no_slip_wall("-Y")
+        b.velocity_BC("+Y", u=req.speed, v=0.0, w=0.0)
+    else:
+        b.velocity_BC("-X", u=req.speed, v=0.0, w=0.0)
+        b.pressure_BC("+X", p=0.0)
+        b.no_slip_wall("-Y")
+        b.no_slip_wall("+Y")
+    b.slip_wall("-Z")
+    b.slip_wall("+Z")
+    model.finalize()
+    solver = IncompressibleSolver(model, 0.7, 0.3)
+    solver.verbose = False
+    solver.vel_equation.tol = atol
+    solver.p_corr_equation.tol = atol
+    solver.vel_equation.max_iter = maxiter
+    solver.p_corr_equation.max_iter = maxiter
+    return model, solver
+
+
+def case_bytes(model, solver) -> int:
+    """Device bytes held by one admitted case (fields, geometry, systems, workspaces)."""
+    ts = [model.cell_values, model.cell_gradients, model.face_values, model.face_gradients, model.mass_fluxes,
+          model.boundary_type, model.boundary_value, solver.rUA, solver.rUA_faces, solver.div_u,
+          solver.vel_correction, solver.stats]
+    ts += [v for v in model._geo.values() if isinstance(v, torch.Tensor)]
+    for e in (solver.vel_equation, solver.p_corr_equation):
+        ts += [e.diag, e.off, e.rhs, e.x, e.ws_vec, e.ws_partials, e.ws_results, e.ws_barrier, e.stats]
+    return int(sum(t.numel() * t.element_size() for t in ts))
+
+
+def estimate_bytes(cells: int) -> int:
+    """Admission estimate before building: about 1.1 kB per cell for a 2D-extruded hex case
+    plus fixed workspaces (measured with case_bytes on the mix's meshes)."""
+    return int(1100 * cells + 2 * 8 * 2048 * 8 + 64 * 1024)
+
+
+@dataclass
+class _Slot:
+    req: Request
+    model: object
+    solver: object
+    bytes: int
+    admitted: float
+    iterations: int = 0
+
+
+@dataclass
+class ServeReport:
+    results: list = field(default_factory=list)
+    wall: float = 0.0
+    cell_iterations: int = 0
+    max_active: int = 0
+    peak_bytes: int = 0
+
+    def summary(self):
+        lat = np.array([r.latency for r in self.results]) if self.results else np.zeros(1)
+        return {
+            "requests": len(self.results),
+            "converged": int(sum(r.converged for r in self.results)),
+            "p50_s": float(np.percentile(lat, 50)),
+            "p99_s": float(np.percentile(lat, 99)),
+            "cell_iterations_per_s": self.cell_iterations / max(self.wall, 1e-9),
+            "wall_s": self.wall,
+            "max_active": self.max_active,
+            "peak_case_bytes": self.peak_bytes,
+        }
+
+
+class Server:
+    """Continuous batching over size buckets (bucket = cell count up to its bound)."""
+
+    def __init__(self, hbm_budget=16 << 30, max_active=96, tol=1e-6, check_every=10, max_outer=4000,
+                 buckets=(4096, 16384, 65536), atol=1e-8, device=None, clock=time.perf_counter,
+                 keep_fields=False):
+        self.budget = int(hbm_budget)
+        self.max_active = int(max_active)
+        self.tol = float(tol)
+        self.check_every = int(check_every)
+        self.max_outer = int(max_outer)
+        self.bounds = tuple(sorted(buckets))
+        self.atol = atol
+        self.device = device or torch.device("cuda", torch.cuda.current_device())
+        self.clock = clock
+        self.meshes = MeshCache()
+        self.keep_fields = keep_fields
+        self.streams = [torch.cuda.Stream(device=self.device) for _ in self.bounds]
+        # one cluster size per bucket, from its bound, so a case's arithmetic never depends
+        # on which other cases share its batch
+        from . import _lib
+        import ctypes as ct
+        lib = _lib.load()
+        self.cluster_sizes = []
+        for b in self.bounds:
+            d = _lib.BatchDims_t(b, 8 * b, 6, 4, 1, 1, 0, 0)
+            self.cluster_sizes.append(int(lib.wcfd_batch_cluster_size(ct.byref(d))))
+
+    def _bucket(self, cells):
+        for i, b in enumerate(self.bounds):
+            if cells <= b:
+                return i
+        return len(self.bounds) - 1
+
+    def run(self, requests) -> ServeReport:
+        pending = sorted(requests, key=lambda r: r.arrival)
+        active = [[] for _ in self.bounds]
+        batches = [None for _ in self.bounds]
+        used = 0
+        report = ServeReport()
+        t0 = self.clock()
+        qi = 0
+        while qi < len(pending) or any(active):
+            now = self.clock() - t0
+            # admit arrived requests while slots and memory allow
+            admitted = False
+            while qi < len(pending) and pending[qi].arrival <= now:
+                req = pending[qi]
+                n_active = sum(len(a) for a in active)
+                if n_active >= self.max_active or used + estimate_bytes(req.cells) > self.budget:
+                    break
+                mesh = self.meshes.get(req.kind, req.cells)
+                model, solver = build_solver(req, mesh, atol=self.atol, device=self.device)
+                nb = case_bytes(model, solver)
+                used += nb
+                report.peak_bytes = max(report.peak_bytes, used)
+                bi = self._bucket(model.num_cells)
+                active[bi].append(_Slot(req, model, solver, nb, self.clock() - t0))
+                batches[bi] = None
+                qi += 1
+                admitted = True
+            n_active = sum(len(a) for a in active)
+            report.max_active = max(report.max_active, n_active)
+            if n_active == 0:
+                # idle until the next arrival
+                wait = pending[qi].arrival - (self.clock() - t0)
+                if wait > 0:
+                    time.sleep(min(wait, 0.01))
+                continue
+            for bi, slots in enumerate(active):
+                if slots and batches[bi] is None:
+                    batches[bi] = CaseBatch([s.solver for s in slots], cluster_size=self.cluster_sizes[bi])
+            # advance every bucket by check_every outer iterations, buckets overlapping
+            for bi, slots in enumerate(active):
+                if not slots:
+                    continue
+                self.streams[bi].wait_stream(torch.cuda.current_stream(self.device))
+                with torch.cuda.stream(self.streams[bi]):
+                    for _ in range(self.check_every):
+                        batches[bi].step()
+            torch.cuda.synchronize(self.device)
+            # retire converged (or exhausted) cases
+            for bi, slots in enumerate(active):
+                if not slots:
+                    continue
+                res = batches[bi].relative_residuals()
+                keep = []
+                for s, r in zip(slots, res):
+                    s.iterations += self.check_every
+                    report.cell_iterations += s.model.num_cells * self.check_every
+                    done = bool(r < self.tol)
+                    if done or s.iterations >= self.max_outer:
+                        report.results.append(Result(s.req.rid, s.req.kind, s.model.num_cells, s.iterations, done,
+                                                     float(r), s.req.arrival, s.admitted, self.clock() - t0,
+                                                     s.model.cell_values.clone() if self.keep_fields else None))
+                        used -= s.bytes
+                    else:
+                        keep.append(s)
+                if len(keep) != len(slots):
+                    active[bi] = keep
+                    batches[bi] = None
+        report.wall = self.clock() - t0
+        return report
+
+
+def run_drop_in(requests, tol=1e-6, check_every=10, max_outer=4000, atol=1e-8, device=None):
+    """The same requests through the plain drop-in path, one case at a time in arrival
+    order: the baseline the batched server is compared with."""
+    meshes = MeshCache()
+    cell_iters = 0
+    t0 = time.perf_counter()
+    results = []
+    for req in sorted(requests, key=lambda r: r.arrival):
+        model, solver = build_solver(req, meshes.get(req.kind, req.cells), atol=atol, device=device)
+        it = 0
+        r = float("inf")
+        while it < max_outer:
+            for _ in range(check_every):
+                solver.step()
+            it += check_every
+            st = solver.solve_stats()[0]
+            r = st["initial_residual"] / max(st["rhs_norm"], 1e-300)
+            if r < tol:
+                break
+        cell_iters += model.num_cells * it
+        results.append((req.rid, it, r))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    return {"cell_iterations_per_s": cell_iters / wall, "wall_s": wall, "results": results}
