@@ -253,20 +253,24 @@ def test_cylinder_piso_with_correction_tracks_oracle():
         b.slip_wall("-Z")
         b.slip_wall("+Z")
 
-    # at the reference's atol (1e-5) this pressure solve stops far from its solution (|p|
-    # 208 vs 78 converged) and fp32/fp64 oracle runs already differ by 3%, so both sides
-    # solve to atol 1e-7 here
+    # This pressure system is poorly conditioned (Neumann walls and cylinder, a weak outlet
+    # Dirichlet row, coefficients scaled by dt): a Krylov stop at atol 1e-7 reduces the
+    # residual only ~1e4 times, so p is fixed to about a percent by the solver tolerance
+    # while u, v are fixed to ~1e-5.  Velocity is held to 1e-4; p to three times the spread
+    # between fp32 and fp64 oracle runs of the same method and tolerance.
     model, solver, oc = make_pair(m, bc, nu=1e-3, ref_cell=None, steady=False, dt=5e-4, correction=True,
                                   inner=2, atol=1e-7)
+    from oracle.simple_ref import OracleCase, geometry_from_mesh
+    b = model.boundary
+    oc64 = OracleCase(geometry_from_mesh(m), b.boundary_type, b.boundary_values, 1e-3, 1.0, T=np.float64,
+                      correction=True, atol=1e-7)
     for it in range(3):
         solver.step()
         oracle_step(oc, None, None, steady=False, dt=5e-4, inner=2)
+        oracle_step(oc64, None, None, steady=False, dt=5e-4, inner=2)
         gv = fields(model)
         for o in (0, 1):
             assert vel_err(gv, oc.cell_values, o) < 1e-4, (it, o)
-        # the constant mode of this pressure system is tied down only by the outlet faces and
-        # is the last mode CG resolves; the velocity correction sees grad p only, so p is
-        # compared up to its mean
-        pg = gv[:, 3] - gv[:, 3].mean()
-        po = oc.cell_values[:, 3] - oc.cell_values[:, 3].mean()
-        assert rel_l2(pg, po) < 1e-3, (it, solver.solve_stats(), oc.log[-1])
+        spread = rel_l2(oc.cell_values[:, 3], oc64.cell_values[:, 3])
+        got = rel_l2(gv[:, 3], oc.cell_values[:, 3])
+        assert got < 3 * spread + 1e-4, (it, got, spread, solver.solve_stats(), oc.log[-1])

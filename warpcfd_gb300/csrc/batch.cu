@@ -20,7 +20,8 @@ int batch_budget_rows(int W) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     const long long budget = (long long)optin - 4096;  // static shared memory and reserve
-    return budget > 0 ? (int)(budget / (8LL * W + 24)) : 0;
+    const long long r = budget > 0 ? budget / (6LL * W + 28) : 0;
+    return (int)(r < 4096 ? r : 4096);  // 12-bit local index of the packed columns
 }
 
 int pick_cluster(const wcfd_batch_dims& d) {

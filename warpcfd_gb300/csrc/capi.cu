@@ -123,7 +123,8 @@ int try_cluster_cg(const wcfd_mesh* m, wcfd_system A, float* x, double atol, int
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     const long long budget = (long long)optin - 8192;  // static shared memory and reserve
     if (budget <= 0) return -1;
-    const long long rmax = budget / (8LL * W + 28);
+    long long rmax = budget / (6LL * W + 28);
+    if (rmax > 4096) rmax = 4096;  // 12-bit local index of the packed columns
     int cs = 0, R = 0;
     for (int c = 1; c <= 16; c *= 2) {
         const long long r = (C + c - 1) / c;

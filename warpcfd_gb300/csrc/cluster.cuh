@@ -79,4 +79,43 @@ __device__ __forceinline__ void cluster_allreduce(ff (&acc)[NV], double (&out)[N
     for (int i = 0; i < NV; ++i) out[i] = res[i];
 }
 
+// Sum NV float-float accumulators over the CTAs of the cluster.  The result (fp64) is left
+// in thread 0 of every CTA only (the same bits in every CTA); the caller derives its
+// scalars there and broadcasts them with one __syncthreads.  Costs one __syncthreads and
+// one cluster barrier: warps merge by butterfly shuffles, warp 0 merges the warp totals
+// and stores the CTA total into slot `me` of every CTA (DSMEM), and after the barrier
+// warp 0 merges the cs slots in rank order.  wsum [2][NV][32] and slots [2][NV][16] are
+// double-buffered by `parity`.
+template <int NV>
+__device__ __forceinline__ void cluster_reduce_to_thread0(ff (&acc)[NV], double (&out)[NV], ff* wsum, ff* slots,
+                                                          unsigned parity, unsigned me, unsigned cs) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) ff_shfl_merge(acc[i], o);
+        if (lane == 0) wsum[(parity * NV + i) * 32 + wid] = acc[i];
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            ff x = lane < CBS / 32 ? wsum[(parity * NV + i) * 32 + lane] : ff_zero();
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) ff_shfl_merge(x, o);
+            if ((unsigned)lane < cs) st_cluster_v2f32(map_rank(slots + (parity * NV + i) * 16 + me, lane), x.hi, x.lo);
+        }
+    }
+    cluster_sync_all();
+    if (wid == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            ff y = (unsigned)lane < cs ? slots[(parity * NV + i) * 16 + lane] : ff_zero();
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) ff_shfl_merge(y, o);
+            if (lane == 0) out[i] = ff_to_double(y);
+        }
+    }
+}
+
 }  // namespace wcfd

@@ -22,14 +22,15 @@
 
 namespace wcfd {
 
-// dynamic shared memory per CTA for R rows and width W:
-// off + packed columns (8 W) and diag, invd, r, p (two buffers), q (24); x stays in global
-// memory (own rows only, coalesced) so 16 CTAs hold 65536 rows of width 4
-size_t cluster_cg_smem_bytes(int R, int W) { return (size_t)R * (8 * (size_t)W + 24); }
+// dynamic shared memory per CTA for R rows and width W: off (4 W), 16-bit packed columns
+// (2 W), diag, invd, r, z, p (two buffers), q (28).  x stays in global memory (own rows,
+// coalesced).  R <= 4096, so 16 CTAs hold 65536 rows of width 4.
+size_t cluster_cg_smem_bytes(int R, int W) { return (size_t)R * (6 * (size_t)W + 28); }
 
 template <int W>
 __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
     extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ ff wsum[2 * 3 * 32];
     __shared__ ff slots[2 * 3 * 16];
     struct Scal {
         double rr, rz, rr0, bb;
@@ -42,49 +43,51 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
     const unsigned cs = cluster_nranks();
     const int row0 = (int)me * R;
     const int nloc = max(0, min(R, C - row0));
-    float* off = reinterpret_cast<float*>(smem);                 // [W][R]
-    uint32_t* colp = reinterpret_cast<uint32_t*>(off + (size_t)W * R);  // [W][R] (rank << 24) | local
-    float* diag = reinterpret_cast<float*>(colp + (size_t)W * R);
+    float* off = reinterpret_cast<float*>(smem);                          // [W][R]
+    float* diag = off + (size_t)W * R;
     float* invd = diag + R;
     float* r = invd + R;
-    float* x = a.x + row0;  // global, own rows
-    float* pbuf0 = r + R;
+    float* z = r + R;
+    float* pbuf0 = z + R;
     float* pbuf1 = pbuf0 + R;
     float* q = pbuf1 + R;
+    uint16_t* colp = reinterpret_cast<uint16_t*>(q + R);                // [W][R] (rank << 12) | local
+    float* x = a.x + row0;                                                // global, own rows
 
-    // load this CTA's slice
+    // load this CTA's slice of the matrix
     for (int l = threadIdx.x; l < nloc; l += CBS) {
         const int g = row0 + l;
-        diag[l] = a.A.diag[g];
-        invd[l] = diag[l] != 0.0f ? 1.0f / diag[l] : 1.0f;
+        const float d = a.A.diag[g];
+        diag[l] = d;
+        invd[l] = d != 0.0f ? 1.0f / d : 1.0f;
 #pragma unroll
         for (int j = 0; j < W; ++j) {
             off[(size_t)j * R + l] = a.A.off[(size_t)j * C + g];
             const int c = a.m.ell_col[(size_t)j * C + g];
             const int rk = c / R;
-            colp[(size_t)j * R + l] = ((uint32_t)rk << 24) | (uint32_t)(c - rk * R);
+            colp[(size_t)j * R + l] = (uint16_t)((rk << 12) | (c - rk * R));
         }
     }
-    cluster_sync_all();
-    // r = b - A x ; p = z = M r ; rr ; rz ; bb
+    // r = b - A x (x read from global) ; z = M r ; p = z ; rr ; rz ; bb
     ff acc[3] = {ff_zero(), ff_zero(), ff_zero()};
     for (int l = threadIdx.x; l < nloc; l += CBS) {
         float ax = diag[l] * x[l];
 #pragma unroll
         for (int j = 0; j < W; ++j) ax += off[(size_t)j * R + l] * a.x[a.m.ell_col[(size_t)j * C + row0 + l]];
-        const float ri = a.A.rhs[row0 + l] - ax;
+        const float bi = a.A.rhs[row0 + l];
+        const float ri = bi - ax;
         const float zi = ri * invd[l];
         r[l] = ri;
+        z[l] = zi;
         pbuf0[l] = zi;
         ff_fma(acc[0], ri, ri);
         ff_fma(acc[1], ri, zi);
-        ff_fma(acc[2], a.A.rhs[row0 + l], a.A.rhs[row0 + l]);
+        ff_fma(acc[2], bi, bi);
     }
     unsigned parity = 0;
     double red[3];
-    cluster_allreduce<3>(acc, red, slots, parity, me, cs);
+    cluster_reduce_to_thread0<3>(acc, red, wsum, slots, parity, me, cs);
     parity ^= 1u;
-    // fp64 scalar work by thread 0 only (fp64 runs at ~1/64 of the fp32 rate on GB300)
     if (threadIdx.x == 0) {
         sc.rr = red[0];
         sc.rr0 = red[0];
@@ -99,26 +102,34 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
     int cur = 0;
     while (sc.go) {
         const float bf = sc.bf;
-        float* po = cur ? pbuf1 : pbuf0;
+        const float* po = cur ? pbuf1 : pbuf0;
         float* pn = cur ? pbuf0 : pbuf1;
+        // p = z + beta p_old (here and for each neighbour) ; q = A p ; p.q
         ff accq[1] = {ff_zero()};
         for (int l = threadIdx.x; l < nloc; l += CBS) {
-            const float pi = r[l] * invd[l] + bf * po[l];
+            const float pi = z[l] + bf * po[l];
             float qi = diag[l] * pi;
 #pragma unroll
             for (int j = 0; j < W; ++j) {
-                const uint32_t cp = colp[(size_t)j * R + l];
-                const float rc = ld_col(r, cp, me);
-                const float dc = ld_col(invd, cp, me);
-                const float pc = ld_col(po, cp, me);
-                qi += off[(size_t)j * R + l] * (rc * dc + bf * pc);
+                const unsigned cp = colp[(size_t)j * R + l];
+                const unsigned rk = cp >> 12;
+                const unsigned lo = cp & 0xFFFu;
+                float zc, pc;
+                if (rk == me) {
+                    zc = z[lo];
+                    pc = po[lo];
+                } else {
+                    zc = ld_cluster_f32(map_rank(z + lo, rk));
+                    pc = ld_cluster_f32(map_rank(po + lo, rk));
+                }
+                qi += off[(size_t)j * R + l] * (zc + bf * pc);
             }
             pn[l] = pi;
             q[l] = qi;
             ff_fma(accq[0], pi, qi);
         }
         double pq[1];
-        cluster_allreduce<1>(accq, pq, slots, parity, me, cs);
+        cluster_reduce_to_thread0<1>(accq, pq, wsum, slots, parity, me, cs);
         parity ^= 1u;
         if (threadIdx.x == 0) {
             if (pq[0] == 0.0) {
@@ -131,17 +142,19 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
         __syncthreads();
         if (!sc.go) break;
         const float af = sc.af;
+        // x += alpha p ; r -= alpha q ; z = M r ; rr ; rz
         ff acc2[2] = {ff_zero(), ff_zero()};
         for (int l = threadIdx.x; l < nloc; l += CBS) {
             x[l] += af * pn[l];
             const float ri = r[l] - af * q[l];
-            r[l] = ri;
             const float zi = ri * invd[l];
+            r[l] = ri;
+            z[l] = zi;
             ff_fma(acc2[0], ri, ri);
             ff_fma(acc2[1], ri, zi);
         }
         double red2[2];
-        cluster_allreduce<2>(acc2, red2, slots, parity, me, cs);
+        cluster_reduce_to_thread0<2>(acc2, red2, wsum, slots, parity, me, cs);
         parity ^= 1u;
         if (threadIdx.x == 0) {
             sc.rr = red2[0];
