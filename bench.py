@@ -177,7 +177,7 @@ class ClockSampler:
             return self
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                                       "--format=csv,noheader,nounits", "-lms", "100"], stdout=subprocess.PIPE,
+                                       "--format=csv,noheader,nounits", "-lms", "50"], stdout=subprocess.PIPE,
                                       stderr=subprocess.DEVNULL, text=True)
         except (FileNotFoundError, OSError):
             self.p = None

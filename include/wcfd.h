@@ -133,6 +133,9 @@ typedef struct wcfd_params {
     int32_t skew;           /* skew correction in face interpolation (1)          */
     double  atol_u;         /* momentum BiCGSTAB absolute tolerance               */
     double  atol_p;         /* pressure CG absolute tolerance                     */
+    int32_t p_refine;       /* fp64 iterative-refinement sweeps of the pressure solve; 0 = off */
+    int32_t pad_;
+    double  p_refine_rtol;  /* relative tolerance of each sweep's fp32 CG correction solve */
 } wcfd_params;
 
 /* a full case: everything one SIMPLE iteration touches */
@@ -147,6 +150,8 @@ typedef struct wcfd_case {
     float*         rua;        /* [C]   rUA = V/(a_P rho)                             */
     float*         rua_faces;  /* [K]                                                */
     float*         div;        /* [C]   div of the mass flux                          */
+    double*        p_x64;      /* [C]   fp64 pressure solution (p_refine > 0 only)       */
+    float*         p_work;     /* [2C]  refinement residual and correction (p_refine > 0) */
     wcfd_krylov_ws ws_u;       /* momentum workspace (ncomp 3)                        */
     wcfd_krylov_ws ws_p;       /* pressure workspace (ncomp 1)                        */
     wcfd_solve_stats* stats;   /* [2]: [0] momentum, [1] pressure (last corrector)    */
@@ -217,6 +222,15 @@ int wcfd_spmv(const wcfd_mesh* m, wcfd_system A, const float* x, float* y, void*
  * or maxiter. */
 int wcfd_cg(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, double atol,
             int32_t maxiter, wcfd_solve_stats* stats, void* stream);
+/* fp64 iterative refinement of a scalar solve (the precision form of the pressure solve):
+ * x64 (fp64, warm start in, result out; x32 receives its fp32 copy).  Each of `sweeps`
+ * sweeps computes r = b - A x64 in fp64, solves A d = r with the fp32 CG (wcfd_cg's
+ * kernels) down to ||r_d|| <= inner_rtol ||r|| or maxiter, and adds d to x64.  work holds
+ * 2 C floats.  `stats` describes the last sweep's correction solve: its initial_residual is
+ * ||b - A x64|| (fp32-rounded) before that sweep. */
+int wcfd_cg_refine(const wcfd_mesh* m, wcfd_system A, double* x64, float* x32, float* work, wcfd_krylov_ws ws,
+                   int32_t sweeps, double inner_rtol, int32_t maxiter, wcfd_solve_stats* stats, void* stream);
+
 /* Which CG kernel wcfd_cg runs: 0 = automatic (the cluster-resident kernel when the system
  * fits in the shared memory of one cluster of up to 16 CTAs, else the grid-cooperative
  * kernel), 1 = always grid-cooperative, 2 = cluster-resident when it fits.  Process-wide. */

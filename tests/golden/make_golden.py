@@ -5,6 +5,8 @@
 ldc64_fp64_converged.npz : 64x64x1 cavity, Re 100, SIMPLE 0.7/0.3, fp64 fields and
                            reductions, Krylov atol 1e-10, 1500 outer iterations
                            (steady state reached; changes < 1e-9 per 100 iterations).
+ldc64_fp32_converged.npz : the same converged run in fp32 fields (fp64 reductions),
+                           atol 1e-7: with the fp64 run it measures the fp32 floor.
 ldc64_fp32_500.npz       : the same case at the reference's own settings (fp32,
                            atol 1e-5, maxiter 500, 500 outer iterations) -- the numbers
                            the reference's configuration produces with this algorithm.
@@ -25,6 +27,7 @@ from tests.cases import cavity_bc, cavity_mesh, host_boundary  # noqa: E402
 
 SPECS = {
     "ldc64_fp64_converged": dict(T=np.float64, atol=1e-10, iters=1500),
+    "ldc64_fp32_converged": dict(T=np.float32, atol=1e-7, iters=1500),
     "ldc64_fp32_500": dict(T=np.float32, atol=1e-5, iters=500),
     "ldc64_fp64_500": dict(T=np.float64, atol=1e-6, iters=500),
 }

@@ -55,6 +55,11 @@ class IncompressibleSolver:
         self.NUM_INNER_LOOPS = 1
         self.steps_done = 0
         self.verbose = True
+        # precision form: fp64 iterative refinement of the pressure solve (0 = off)
+        self.p_refine = 0
+        self.p_refine_rtol = 1e-3
+        self.p_x64 = None
+        self.p_work = None
         self._graph = None
         self._graph_key = None
         self._mesh_t = model.mesh_struct(correction=correction)
@@ -95,14 +100,15 @@ class IncompressibleSolver:
                              -1 if ref is None else int(ref), int(steady), int(self.NUM_INNER_LOOPS),
                              int(self.NUM_ORTHOGONAL_CORRECTORS), int(self.vel_equation.max_iter),
                              int(bool(m.skew_correction)), float(self.vel_equation.tol),
-                             float(self.p_corr_equation.tol))
+                             float(self.p_corr_equation.tol), int(self.p_refine), 0, float(self.p_refine_rtol))
 
     def _param_key(self):
         m = self.model
         return (self.material.density, self.material.viscosity, self.steady_state, self.u_relaxation_factor,
                 self.p_relaxation_factor, self.dt, m.reference_pressure_cell_id, m.reference_pressure,
                 self.NUM_INNER_LOOPS, self.NUM_ORTHOGONAL_CORRECTORS, self.vel_equation.max_iter,
-                m.skew_correction, self.vel_equation.tol, self.p_corr_equation.tol, self._events_ptr)
+                m.skew_correction, self.vel_equation.tol, self.p_corr_equation.tol, self._events_ptr,
+                self.p_refine, self.p_refine_rtol)
 
     def case_struct(self) -> _lib.Case_t:
         """The C struct of this case; rebuilt only when a parameter changed (the device
@@ -116,9 +122,15 @@ class IncompressibleSolver:
     def _build_case_struct(self) -> _lib.Case_t:
         m = self.model
         ve, pe = self.vel_equation, self.p_corr_equation
+        if self.p_refine > 0 and self.p_x64 is None:
+            self.p_x64 = pe.x.to(torch.float64)
+            self.p_work = torch.zeros(2 * m.num_cells, dtype=torch.float32, device=m.device)
         return _lib.Case_t(self._mesh_t, m.bc_struct(), m.state_struct(), ve.system_struct(), pe.system_struct(),
                            self.HbyA.data_ptr(), pe.x.data_ptr(), self.rUA.data_ptr(), self.rUA_faces.data_ptr(),
-                           self.div_u.data_ptr(), ve.workspace_struct(), pe.workspace_struct(),
+                           self.div_u.data_ptr(),
+                           self.p_x64.data_ptr() if self.p_x64 is not None else None,
+                           self.p_work.data_ptr() if self.p_work is not None else None,
+                           ve.workspace_struct(), pe.workspace_struct(),
                            self.stats.data_ptr(), self.params(), self._events_ptr)
 
     # ------------------------------------------------------------------ stepping

@@ -71,12 +71,13 @@ class Params_t(ct.Structure):
     _fields_ = [("nu", ct.c_float), ("rho", ct.c_float), ("u_relax", ct.c_float), ("p_relax", ct.c_float),
                 ("dt", ct.c_float), ("ref_value", ct.c_float), ("ref_cell", ct.c_int32), ("steady", ct.c_int32),
                 ("n_inner", ct.c_int32), ("n_ortho", ct.c_int32), ("maxiter", ct.c_int32), ("skew", ct.c_int32),
-                ("atol_u", ct.c_double), ("atol_p", ct.c_double)]
+                ("atol_u", ct.c_double), ("atol_p", ct.c_double), ("p_refine", ct.c_int32), ("pad_", ct.c_int32),
+                ("p_refine_rtol", ct.c_double)]
 
 
 class Case_t(ct.Structure):
     _fields_ = [("mesh", Mesh_t), ("bc", BC_t), ("state", State_t), ("mom", System_t), ("pres", System_t),
-                ("hbya", vp), ("p_x", vp), ("rua", vp), ("rua_faces", vp), ("div", vp),
+                ("hbya", vp), ("p_x", vp), ("rua", vp), ("rua_faces", vp), ("div", vp), ("p_x64", vp), ("p_work", vp),
                 ("ws_u", KrylovWS_t), ("ws_p", KrylovWS_t), ("stats", vp), ("prm", Params_t),
                 ("events", vp)]
 
@@ -107,6 +108,8 @@ _SIGS = {
     "wcfd_bicgstab": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, KrylovWS_t, ct.c_double, ct.c_int32, vp, vp]),
     "wcfd_simple_iteration": (ct.c_int, [ct.POINTER(Case_t), vp]),
     "wcfd_set_krylov_path": (ct.c_int, [ct.c_int32]),
+    "wcfd_cg_refine": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, vp, vp, KrylovWS_t, ct.c_int32, ct.c_double,
+                                  ct.c_int32, vp, vp]),
     "wcfd_cg_noalloc": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, ct.c_double, ct.c_int32, vp, vp]),
     "wcfd_batch_cluster_size": (ct.c_int, [ct.POINTER(BatchDims_t)]),
     "wcfd_batch_simple_iteration": (ct.c_int, [vp, ct.c_int32, ct.POINTER(BatchDims_t), vp]),

@@ -73,7 +73,8 @@ int coop_capacity(const void* fn, int /*unused*/) {
 }
 
 int launch_krylov(const void* fn, int slot, const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws,
-                  double atol, int maxiter, wcfd_solve_stats* stats, cudaStream_t st, const char* name) {
+                  double atol, int maxiter, wcfd_solve_stats* stats, cudaStream_t st, const char* name,
+                  double rtol = 0.0) {
     int rc = check_mesh(m);
     if (rc) return rc;
     RET_IF(!fn, WCFD_ERR_ARGUMENT, "no solver kernel for this off-diagonal width");
@@ -88,7 +89,7 @@ int launch_krylov(const void* fn, int slot, const wcfd_mesh* m, wcfd_system A, f
     if (grid < 1) grid = 1;
     if (cudaMemsetAsync(ws.barrier, 0, WCFD_BARRIER_WORDS * sizeof(uint32_t), st) != cudaSuccess)
         return set_error(WCFD_ERR_CUDA, "barrier reset failed");
-    KrylovArgs a;
+    KrylovArgs a = {};
     a.m = *m;
     a.A = A;
     a.x = x;
@@ -97,6 +98,7 @@ int launch_krylov(const void* fn, int slot, const wcfd_mesh* m, wcfd_system A, f
     a.g.flags = ws.barrier;
     a.g.err = reinterpret_cast<int*>(ws.barrier + WCFD_MAX_BLOCKS);
     a.atol2 = atol * atol;
+    a.rtol2 = rtol * rtol;
     a.maxiter = maxiter;
     a.stats = stats;
     void* args[] = {&a};
@@ -114,7 +116,7 @@ int g_krylov_path = 0;  // 0 automatic, 1 grid-cooperative only, 2 cluster-resid
 // Cluster-resident CG when the system fits in the shared memory of one cluster of up to
 // 16 CTAs; returns -1 (caller falls back to the grid-cooperative kernel) otherwise.
 int try_cluster_cg(const wcfd_mesh* m, wcfd_system A, float* x, double atol, int maxiter,
-                   wcfd_solve_stats* stats, cudaStream_t st) {
+                   wcfd_solve_stats* stats, cudaStream_t st, double rtol = 0.0) {
     if (g_krylov_path == 1) return -1;
     const int C = m->n_cells, W = m->ell_width;
     int dev = 0;
@@ -187,6 +189,7 @@ int try_cluster_cg(const wcfd_mesh* m, wcfd_system A, float* x, double atol, int
     a.A = A;
     a.x = x;
     a.atol2 = atol * atol;
+    a.rtol2 = rtol * rtol;
     a.maxiter = maxiter;
     a.stats = stats;
     void* args[] = {&a, &R};
@@ -312,16 +315,53 @@ int wcfd_spmv(const wcfd_mesh* m, wcfd_system A, const float* x, float* y, void*
     return WCFD_OK;
 }
 
-int wcfd_cg(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, double atol, int32_t maxiter,
-            wcfd_solve_stats* stats, void* stream) {
+static int cg_solve(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, double atol, double rtol,
+                    int32_t maxiter, wcfd_solve_stats* stats, void* stream) {
     RET_IF(A.ncomp != 1, WCFD_ERR_ARGUMENT, "cg solves scalar systems (ncomp 1)");
     int rc = check_mesh(m);
     if (rc) return rc;
     RET_IF(!A.diag || !A.off || !A.rhs || !x || !stats, WCFD_ERR_ARGUMENT, "null solver argument");
-    RET_IF(maxiter < 0 || !(atol >= 0.0), WCFD_ERR_ARGUMENT, "bad atol or maxiter");
-    rc = try_cluster_cg(m, A, x, atol, maxiter, stats, S(stream));
+    RET_IF(maxiter < 0 || !(atol >= 0.0) || !(rtol >= 0.0), WCFD_ERR_ARGUMENT, "bad tolerance or maxiter");
+    rc = try_cluster_cg(m, A, x, atol, maxiter, stats, S(stream), rtol);
     if (rc >= 0) return rc;
-    return launch_krylov(cg_kernel_for(m->ell_width), 0, m, A, x, ws, atol, maxiter, stats, S(stream), "cg_kernel");
+    return launch_krylov(cg_kernel_for(m->ell_width), 0, m, A, x, ws, atol, maxiter, stats, S(stream), "cg_kernel",
+                         rtol);
+}
+
+int wcfd_cg(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, double atol, int32_t maxiter,
+            wcfd_solve_stats* stats, void* stream) {
+    return cg_solve(m, A, x, ws, atol, 0.0, maxiter, stats, stream);
+}
+
+int wcfd_cg_refine(const wcfd_mesh* m, wcfd_system A, double* x64, float* x32, float* work, wcfd_krylov_ws ws,
+                   int32_t sweeps, double inner_rtol, int32_t maxiter, wcfd_solve_stats* stats, void* stream) {
+    int rc = check_mesh(m);
+    if (rc) return rc;
+    RET_IF(!x64 || !x32 || !work || sweeps < 1 || !(inner_rtol > 0.0 && inner_rtol < 1.0), WCFD_ERR_ARGUMENT,
+           "bad refinement arguments");
+    const void* res_fn = residual64_kernel_for(m->ell_width);
+    RET_IF(!res_fn, WCFD_ERR_ARGUMENT, "no residual kernel for this width");
+    cudaStream_t st = S(stream);
+    const int C = m->n_cells;
+    float* r = work;
+    float* d = work + C;
+    wcfd_system Ar = A;
+    Ar.rhs = r;
+    const int gc = grid_for(C);
+    for (int sw = 0; sw < sweeps; ++sw) {
+        wcfd_mesh mm = *m;
+        void* rargs[] = {&mm, &A, &x64, &r};
+        if (cudaLaunchKernel(res_fn, dim3(gc), dim3(kBlock), rargs, 0, st) != cudaSuccess) {
+            LAUNCH_CHECK("residual64_kernel");
+        }
+        if (cudaMemsetAsync(d, 0, sizeof(float) * (size_t)C, st) != cudaSuccess)
+            return set_error(WCFD_ERR_CUDA, "refinement memset failed");
+        rc = cg_solve(m, Ar, d, ws, 0.0, inner_rtol, maxiter, stats, stream);
+        if (rc) return rc;
+        refine_update_kernel<<<gc, kBlock, 0, st>>>(C, x64, d, x32);
+        LAUNCH_CHECK("refine_update_kernel");
+    }
+    return WCFD_OK;
 }
 
 int wcfd_bicgstab(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, double atol, int32_t maxiter,
@@ -374,7 +414,11 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
             if (rc) return rc;
             const bool last = inner == c.prm.n_inner - 1 && ortho == c.prm.n_ortho - 1;
             if (last) mark(2);
-            rc = wcfd_cg(&m, c.pres, c.p_x, c.ws_p, c.prm.atol_p, c.prm.maxiter, c.stats + 1, stream);
+            if (c.prm.p_refine > 0)
+                rc = wcfd_cg_refine(&m, c.pres, c.p_x64, c.p_x, c.p_work, c.ws_p, c.prm.p_refine, c.prm.p_refine_rtol,
+                                    c.prm.maxiter, c.stats + 1, stream);
+            else
+                rc = wcfd_cg(&m, c.pres, c.p_x, c.ws_p, c.prm.atol_p, c.prm.maxiter, c.stats + 1, stream);
             if (rc) return rc;
             if (last) mark(3);
             // :144-147

@@ -43,6 +43,7 @@ struct KrylovArgs {
     float* ws;            // workspace vectors
     GridCtl g;
     double atol2;
+    double rtol2;         // CG only: also stop when ||r||^2 <= rtol2 ||r0||^2 (0 = off)
     int maxiter;
     wcfd_solve_stats* stats;
 };
@@ -53,6 +54,8 @@ const void* cg_cluster_kernel_for(int W);
 const void* cg_cluster_batched_for(int W);
 const void* bicgstab_cluster_batched_for(int W);
 size_t cluster_cg_smem_bytes(int R, int W);
+const void* residual64_kernel_for(int W);
+__global__ void refine_update_kernel(int C, double* x64, const float* d, float* x32);
 
 inline int grid_for(long long n, int bs = kBlock) { return (int)((n + bs - 1) / bs); }
 

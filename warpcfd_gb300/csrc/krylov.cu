@@ -27,7 +27,7 @@ __device__ __forceinline__ float jacobi(float d) { return d != 0.0f ? 1.0f / d :
 
 // Krylov scalars of one block, owned by thread 0
 struct KScalars {
-    double rr, rz, rho, alpha, rr0, bb;
+    double rr, rz, rho, alpha, rr0, bb, thr2;
     float af, bf, of;
     int go, status, k;
 };
@@ -56,7 +56,7 @@ __device__ void fail_stats(const KrylovArgs& a, int k) {
 __device__ void write_stats(const KrylovArgs& a, const KScalars& sc) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         int st = sc.status;
-        if (st == WCFD_OK && !(sc.rr <= a.atol2)) st = WCFD_NOT_CONVERGED;
+        if (st == WCFD_OK && !(sc.rr <= sc.thr2)) st = WCFD_NOT_CONVERGED;
         a.stats->iterations = sc.k;
         a.stats->status = st;
         a.stats->residual = sqrt(sc.rr);
@@ -111,9 +111,10 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
         sc.rr = red[0];
         sc.rr0 = red[0];
         sc.bb = red[2];
+        sc.thr2 = fmax(a.atol2, a.rtol2 * red[0]);
         sc.rz = red[1];
         sc.bf = 0.0f;  // the first direction is z itself
-        sc.go = (0 < a.maxiter && red[0] > a.atol2);
+        sc.go = (0 < a.maxiter && red[0] > sc.thr2);
     }
     __syncthreads();
     int cur = 0;
@@ -165,7 +166,7 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
             sc.bf = (float)(sc.rz != 0.0 ? red2[1] / sc.rz : 0.0);
             sc.rz = red2[1];
             sc.k += 1;
-            sc.go = (sc.k < a.maxiter && sc.rr > a.atol2);
+            sc.go = (sc.k < a.maxiter && sc.rr > sc.thr2);
         }
         __syncthreads();
         cur ^= 1;
@@ -233,10 +234,11 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
         sc.rr = red[0];
         sc.rr0 = red[0];
         sc.bb = red[1];
+        sc.thr2 = a.atol2;
         sc.rho = red[0];
         sc.bf = 0.0f;  // the first direction is r itself
         sc.of = 0.0f;
-        sc.go = (0 < a.maxiter && red[0] > a.atol2);
+        sc.go = (0 < a.maxiter && red[0] > sc.thr2);
     }
     __syncthreads();
     int cur = 0;
@@ -351,13 +353,52 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
             } else {
                 sc.bf = (float)((rr2[1] / sc.rho) * (sc.alpha / omega));
                 sc.rho = rr2[1];
-                sc.go = (sc.k < a.maxiter && sc.rr > a.atol2);
+                sc.go = (sc.k < a.maxiter && sc.rr > sc.thr2);
             }
         }
         __syncthreads();
         cur ^= 1;
     }
     write_stats(a, sc);
+}
+
+// ---------------------------------------------------------------------------------
+// fp64 iterative refinement of a scalar solve (the precision form of the pressure solve):
+// the solution is kept in fp64 and each sweep solves for a correction with the fp32 CG
+// against the residual r = b - A x computed in fp64.  The few fp64 operations per row per
+// sweep (not per Krylov iteration) are affordable at GB300's fp64 rate.
+template <int W>
+__global__ void __launch_bounds__(kBlock) residual64_kernel(wcfd_mesh m, wcfd_system A, const double* __restrict__ x,
+                                                            float* __restrict__ r) {
+    const int i = blockIdx.x * kBlock + threadIdx.x;
+    const int C = m.n_cells;
+    if (i >= C) return;
+    double acc = (double)A.diag[i] * x[i];
+#pragma unroll
+    for (int j = 0; j < W; ++j) acc += (double)A.off[(size_t)j * C + i] * x[m.ell_col[(size_t)j * C + i]];
+    r[i] = (float)((double)A.rhs[i] - acc);
+}
+
+__global__ void __launch_bounds__(kBlock) refine_update_kernel(int C, double* __restrict__ x64,
+                                                               const float* __restrict__ d, float* __restrict__ x32) {
+    const int i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= C) return;
+    const double v = x64[i] + (double)d[i];
+    x64[i] = v;
+    x32[i] = (float)v;
+}
+
+const void* residual64_kernel_for(int W) {
+    switch (W) {
+        case 0: return (const void*)residual64_kernel<0>;
+        case 1: return (const void*)residual64_kernel<1>;
+        case 2: return (const void*)residual64_kernel<2>;
+        case 3: return (const void*)residual64_kernel<3>;
+        case 4: return (const void*)residual64_kernel<4>;
+        case 5: return (const void*)residual64_kernel<5>;
+        case 6: return (const void*)residual64_kernel<6>;
+        default: return nullptr;
+    }
 }
 
 const void* cg_kernel_for(int W) {

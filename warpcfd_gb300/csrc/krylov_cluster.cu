@@ -33,7 +33,7 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
     __shared__ ff wsum[2 * 3 * 32];
     __shared__ ff slots[2 * 3 * 16];
     struct Scal {
-        double rr, rz, rr0, bb;
+        double rr, rz, rr0, bb, thr2;
         float af, bf;
         int go, status, k;
     };
@@ -92,11 +92,12 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
         sc.rr = red[0];
         sc.rr0 = red[0];
         sc.bb = red[2];
+        sc.thr2 = fmax(a.atol2, a.rtol2 * red[0]);
         sc.rz = red[1];
         sc.bf = 0.0f;
         sc.k = 0;
         sc.status = WCFD_OK;
-        sc.go = (0 < a.maxiter && red[0] > a.atol2);
+        sc.go = (0 < a.maxiter && red[0] > sc.thr2);
     }
     __syncthreads();
     int cur = 0;
@@ -161,14 +162,14 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
             sc.bf = (float)(sc.rz != 0.0 ? red2[1] / sc.rz : 0.0);
             sc.rz = red2[1];
             sc.k += 1;
-            sc.go = (sc.k < a.maxiter && sc.rr > a.atol2);
+            sc.go = (sc.k < a.maxiter && sc.rr > sc.thr2);
         }
         __syncthreads();
         cur ^= 1;
     }
     if (me == 0 && threadIdx.x == 0) {
         int st = sc.status;
-        if (st == WCFD_OK && !(sc.rr <= a.atol2)) st = WCFD_NOT_CONVERGED;
+        if (st == WCFD_OK && !(sc.rr <= sc.thr2)) st = WCFD_NOT_CONVERGED;
         a.stats->iterations = sc.k;
         a.stats->status = st;
         a.stats->residual = sqrt(sc.rr);
