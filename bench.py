@@ -1,7 +1,7 @@
 """Benchmark of the SIMPLE outer iteration (cell-iterations/s) on GB300.
 
 Default workload: steady channel flow, 400 x 80 x 1 hexes on a 10 x 1 domain, uniform
-inlet u = 1, outlet p = 0, no-slip walls, Re = 200, relaxation 0.7 / 0.3, fp32 fields
+inlet u = 1, outlet p = 0, no-slip walls, Re = 200, relaxation 0.3 / 0.3, fp32 fields
 with fp64 Krylov reductions.  One step = one SIMPLE outer iteration (momentum BiCGSTAB +
 pressure CG, up to 500 iterations each, atol 1e-5).  Synthetic seeded mesh, zero
 initial fields.
@@ -31,12 +31,15 @@ sys.path.insert(0, ROOT)
 
 WORKLOADS = {
     # name: (description, builder args)
-    "channel": "steady channel 400x80x1 hex on 10x1, u_in=1, p_out=0, Re=200, SIMPLE 0.7/0.3, fp32 (fp64 reductions)",
+    "channel": "steady channel 400x80x1 hex on 10x1, u_in=1, p_out=0, Re=200, SIMPLE 0.3/0.3, fp32 (fp64 reductions)",
     "cavity": "lid-driven cavity 64x64x1 hex, lid u=1, Re=100, SIMPLE 0.7/0.3, fp32 (fp64 reductions)",
     "cavity3d": "3D lid-driven cavity 128^3 hex, lid u=1, Re=400, SIMPLE 0.7/0.3, fp32 (fp64 reductions)",
     "cylinder": "cylinder D=0.1 in a 2.2x0.41 channel, 254k jittered hex (O-grid, seed 0), parabolic inlet "
                 "U_max=1.5, Re=100, PISO dt=5e-4 with 2 correctors and non-orthogonal correction, fp32 "
                 "(fp64 reductions); one step = one time step",
+    "serve": "serving mix: steady cavity/channel requests, cells log-uniform in [32^2, 256^2], Re ~ U[50, 1000], "
+             "speed ~ U[0.5, 2], seeded Poisson arrivals, converged to a 1e-6 relative momentum residual; "
+             "continuous batching (batched form) vs the drop-in path one case at a time",
 }
 METRIC = "cell-iterations/s"
 
@@ -64,9 +67,16 @@ def build_mesh(workload):
 
 
 def solver_setup(workload):
-    """(steady, u_relax, p_relax, dt, correctors, non-orthogonal correction) of a workload."""
+    """(steady, u_relax, p_relax, dt, correctors, non-orthogonal correction) of a workload.
+
+    The channel uses the relaxation of the reference's own channel example (0.3 / 0.3,
+    examples/Channel Flow/Channel Flow.py:51): with the cavity's 0.7 / 0.3
+    (examples/LDC/LDC.py:48) the reference method diverges on this channel within a few
+    dozen iterations (no Rhie-Chow face flux, velocity inlet, pressure outlet)."""
     if workload == "cylinder":
         return False, None, None, 5e-4, 2, True
+    if workload == "channel":
+        return True, 0.3, 0.3, 1.0, 1, False
     return True, 0.7, 0.3, 1.0, 1, False
 
 
@@ -262,6 +272,42 @@ def run_reference(args):
     return 0
 
 
+def run_serve(args):
+    """Serving mix through the continuous-batching server; the drop-in path (one case at a
+    time, same settings) runs a bounded sample of the same mix for the comparison."""
+    import torch
+
+    from warpcfd_gb300.build import build_library
+    from warpcfd_gb300.serve import Server, make_request_mix, run_drop_in
+
+    build_library()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    reqs = make_request_mix(args.requests, seed=0, rate=args.rate)
+    # warm-up: a few small requests compile nothing but touch every kernel and the caches
+    Server(max_outer=30).run(make_request_mix(4, seed=1, rate=1e6, lo=32 * 32, hi=48 * 48))
+    torch.cuda.synchronize()
+    with ClockSampler(0, enabled=not args.no_clocks) as clocks:
+        rep = Server(max_outer=args.max_outer).run(reqs)
+    summ = rep.summary()
+    # drop-in on a sample: the first requests in arrival order, same stop settings
+    n_drop = min(args.drop_in_sample, len(reqs))
+    drop = run_drop_in(reqs[:n_drop], max_outer=args.max_outer)
+    line = {
+        "metric": METRIC, "value": summ["cell_iterations_per_s"], "unit": METRIC, "n_gpus": 1, "steps": len(reqs),
+        "warmup": 4, "ms_per_step": 1e3 * summ["wall_s"] / max(len(reqs), 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOADS["serve"], "requests": len(reqs), "arrival_rate_per_s": args.rate,
+                   "max_outer": args.max_outer, "step": "one request served to completion"},
+        "serving": summ,
+        "drop_in": {"requests": n_drop, "cell_iterations_per_s": drop["cell_iterations_per_s"],
+                    "wall_s": drop["wall_s"]},
+        "batched_over_drop_in": summ["cell_iterations_per_s"] / max(drop["cell_iterations_per_s"], 1e-9),
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def run_ours(args):
     import torch
 
@@ -319,6 +365,10 @@ def run_ours(args):
     hist = np.frombuffer(stats_hist.cpu().numpy().tobytes(), dtype=STATS_DTYPE).reshape(K_, 2)
     k_u = hist[:, 0]["iterations"].astype(np.int64)
     k_p = hist[:, 1]["iterations"].astype(np.int64)
+    finite = bool(torch.isfinite(model.cell_values).all().item())
+    if not finite:
+        raise SystemExit("bench: the fields went non-finite during the timed steps; no valid measurement")
+    rel_res = hist[:, 0]["initial_residual"] / np.maximum(hist[:, 0]["rhs_norm"], 1e-300)
     total_ms = float(step_ms.sum())
     if dist is not None:
         t = torch.tensor([total_ms], device="cuda")
@@ -364,7 +414,10 @@ def run_ours(args):
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOADS[args.workload], "cells": C, "faces": K, "l2": "flushed between steps "
                    "(256 MiB write outside the step events)", "parallelism": f"replicas x{world}",
-                   "krylov_iters_mean": {"bicgstab": float(k_u.mean()), "cg": float(k_p.mean())}},
+                   "krylov_iters_mean": {"bicgstab": float(k_u.mean()), "cg": float(k_p.mean())},
+                   "relaxation": [solver.u_relaxation_factor, solver.p_relaxation_factor],
+                   "fields_finite": finite,
+                   "momentum_rel_residual": {"first": float(rel_res[0]), "last": float(rel_res[-1])}},
         "e2e": e2e,
         "gpu_launches": (6 + 7 * solver.NUM_INNER_LOOPS) * K_,
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -395,11 +448,17 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=150.0)
     ap.add_argument("--no-clocks", action="store_true", help="do not sample nvidia-smi during the timed region")
+    ap.add_argument("--requests", type=int, default=256, help="serve workload: requests in the mix")
+    ap.add_argument("--rate", type=float, default=2000.0, help="serve workload: Poisson arrival rate (1/s)")
+    ap.add_argument("--max-outer", type=int, default=4000, help="serve workload: outer-iteration cap per request")
+    ap.add_argument("--drop-in-sample", type=int, default=24, help="serve workload: requests run through the drop-in")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "serve":
+        return run_serve(args)
     return run_ours(args)
 
 

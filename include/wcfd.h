@@ -136,6 +136,8 @@ typedef struct wcfd_params {
     int32_t p_refine;       /* fp64 iterative-refinement sweeps of the pressure solve; 0 = off */
     int32_t pad_;
     double  p_refine_rtol;  /* relative tolerance of each sweep's fp32 CG correction solve */
+    double  rtol_u;         /* momentum stop also at ||r|| <= rtol_u ||r_0||; 0 = atol only (the reference) */
+    double  rtol_p;         /* pressure stop also at ||r|| <= rtol_p ||r_0||; 0 = atol only (the reference) */
 } wcfd_params;
 
 /* a full case: everything one SIMPLE iteration touches */
@@ -237,6 +239,12 @@ int wcfd_cg_refine(const wcfd_mesh* m, wcfd_system A, double* x64, float* x32, f
 int wcfd_set_krylov_path(int32_t path);
 int wcfd_bicgstab(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, double atol,
                   int32_t maxiter, wcfd_solve_stats* stats, void* stream);
+/* wcfd_cg (method 0) or wcfd_bicgstab (method 1) with an added relative stop: the solve
+ * ends at ||r||_2 <= max(atol, rtol ||r_0||_2).  rtol = 0 is exactly wcfd_cg / wcfd_bicgstab.
+ * The reference stops on atol alone; the relative stop lets a steady outer iteration ask
+ * for solves whose accuracy follows its own residual (the serving form uses it). */
+int wcfd_krylov_solve(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, int32_t method,
+                      double atol, double rtol, int32_t maxiter, wcfd_solve_stats* stats, void* stream);
 
 /* Allocation-free variant of wcfd_cg (no counterpart in the reference).  For callers that
  * hold their input and output device arrays but cannot allocate device workspace (device

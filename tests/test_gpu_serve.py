@@ -34,4 +34,4 @@ def test_served_alone_equals_in_mix():
         alone = Server(**kw).run([req]).results[0]
         got = by_id[req.rid]
         assert alone.iterations == got.iterations
-        assert torch.equal(alone.fields, got.fields)
+        assert torch.equal(alone.fields.view(torch.int32), got.fields.view(torch.int32))  # bitwise, NaN too

@@ -45,6 +45,8 @@ class Equation:
         self.fvm = fvm
         self.max_iter = 500
         self.tol = 1.0e-5
+        # relative stop ||r|| <= rtol ||r_0|| on top of tol; 0 = tol alone, as in the reference
+        self.rtol = 0.0
         C = fvm.num_cells
         n = self.num_outputs
         W = fvm._geo["ell_width"]
@@ -128,10 +130,15 @@ class Equation:
         if x is None:
             x = self.x
         m = self.fvm.mesh_struct()
-        fn = "wcfd_bicgstab" if self.linear_solver == "bicgstab" else "wcfd_cg"
-        _lib.call(fn, ct.byref(m), self.system_struct(), ct.c_void_p(x.data_ptr()), self.workspace_struct(),
-                  float(self.tol), int(self.max_iter), ct.c_void_p(self.stats.data_ptr()),
-                  ct.c_void_p(torch.cuda.current_stream().cuda_stream))
+        stream = ct.c_void_p(torch.cuda.current_stream().cuda_stream)
+        if self.rtol > 0.0:
+            _lib.call("wcfd_krylov_solve", ct.byref(m), self.system_struct(), ct.c_void_p(x.data_ptr()),
+                      self.workspace_struct(), int(self.linear_solver == "bicgstab"), float(self.tol),
+                      float(self.rtol), int(self.max_iter), ct.c_void_p(self.stats.data_ptr()), stream)
+        else:
+            fn = "wcfd_bicgstab" if self.linear_solver == "bicgstab" else "wcfd_cg"
+            _lib.call(fn, ct.byref(m), self.system_struct(), ct.c_void_p(x.data_ptr()), self.workspace_struct(),
+                      float(self.tol), int(self.max_iter), ct.c_void_p(self.stats.data_ptr()), stream)
         raw = np.frombuffer(self.stats.cpu().numpy().tobytes(), dtype=_lib.STATS_DTYPE)[0]
         return dict(iterations=int(raw["iterations"]), status=_lib.STATUS_NAMES.get(int(raw["status"]), "?"),
                     residual=float(raw["residual"]), initial_residual=float(raw["initial_residual"]),

@@ -72,7 +72,7 @@ class Params_t(ct.Structure):
                 ("dt", ct.c_float), ("ref_value", ct.c_float), ("ref_cell", ct.c_int32), ("steady", ct.c_int32),
                 ("n_inner", ct.c_int32), ("n_ortho", ct.c_int32), ("maxiter", ct.c_int32), ("skew", ct.c_int32),
                 ("atol_u", ct.c_double), ("atol_p", ct.c_double), ("p_refine", ct.c_int32), ("pad_", ct.c_int32),
-                ("p_refine_rtol", ct.c_double)]
+                ("p_refine_rtol", ct.c_double), ("rtol_u", ct.c_double), ("rtol_p", ct.c_double)]
 
 
 class Case_t(ct.Structure):
@@ -106,6 +106,8 @@ _SIGS = {
     "wcfd_spmv": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, vp, vp]),
     "wcfd_cg": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, KrylovWS_t, ct.c_double, ct.c_int32, vp, vp]),
     "wcfd_bicgstab": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, KrylovWS_t, ct.c_double, ct.c_int32, vp, vp]),
+    "wcfd_krylov_solve": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, KrylovWS_t, ct.c_int32, ct.c_double,
+                                     ct.c_double, ct.c_int32, vp, vp]),
     "wcfd_simple_iteration": (ct.c_int, [ct.POINTER(Case_t), vp]),
     "wcfd_set_krylov_path": (ct.c_int, [ct.c_int32]),
     "wcfd_cg_refine": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, vp, vp, KrylovWS_t, ct.c_int32, ct.c_double,

@@ -364,11 +364,24 @@ int wcfd_cg_refine(const wcfd_mesh* m, wcfd_system A, double* x64, float* x32, f
     return WCFD_OK;
 }
 
+static int bicgstab_solve(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, double atol, double rtol,
+                          int32_t maxiter, wcfd_solve_stats* stats, void* stream) {
+    RET_IF(A.ncomp != 3, WCFD_ERR_ARGUMENT, "bicgstab solves the 3-component momentum system (ncomp 3)");
+    RET_IF(!(rtol >= 0.0), WCFD_ERR_ARGUMENT, "bad rtol");
+    return launch_krylov(bicgstab_kernel_for(m->ell_width), 1, m, A, x, ws, atol, maxiter, stats, S(stream),
+                         "bicgstab_kernel", rtol);
+}
+
 int wcfd_bicgstab(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, double atol, int32_t maxiter,
                   wcfd_solve_stats* stats, void* stream) {
-    RET_IF(A.ncomp != 3, WCFD_ERR_ARGUMENT, "bicgstab solves the 3-component momentum system (ncomp 3)");
-    return launch_krylov(bicgstab_kernel_for(m->ell_width), 1, m, A, x, ws, atol, maxiter, stats, S(stream),
-                         "bicgstab_kernel");
+    return bicgstab_solve(m, A, x, ws, atol, 0.0, maxiter, stats, stream);
+}
+
+int wcfd_krylov_solve(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, int32_t method,
+                      double atol, double rtol, int32_t maxiter, wcfd_solve_stats* stats, void* stream) {
+    RET_IF(method != 0 && method != 1, WCFD_ERR_ARGUMENT, "method must be 0 (cg) or 1 (bicgstab)");
+    if (method == 1) return bicgstab_solve(m, A, x, ws, atol, rtol, maxiter, stats, stream);
+    return cg_solve(m, A, x, ws, atol, rtol, maxiter, stats, stream);
 }
 
 int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
@@ -394,7 +407,7 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
         if (c.events && c.events[i]) cudaEventRecord(reinterpret_cast<cudaEvent_t>(c.events[i]), st);
     };
     mark(0);
-    rc = wcfd_bicgstab(&m, c.mom, c.hbya, c.ws_u, c.prm.atol_u, c.prm.maxiter, c.stats + 0, stream);
+    rc = bicgstab_solve(&m, c.mom, c.hbya, c.ws_u, c.prm.atol_u, c.prm.rtol_u, c.prm.maxiter, c.stats + 0, stream);
     if (rc) return rc;
     mark(1);
     // :118-123
@@ -418,7 +431,7 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
                 rc = wcfd_cg_refine(&m, c.pres, c.p_x64, c.p_x, c.p_work, c.ws_p, c.prm.p_refine, c.prm.p_refine_rtol,
                                     c.prm.maxiter, c.stats + 1, stream);
             else
-                rc = wcfd_cg(&m, c.pres, c.p_x, c.ws_p, c.prm.atol_p, c.prm.maxiter, c.stats + 1, stream);
+                rc = cg_solve(&m, c.pres, c.p_x, c.ws_p, c.prm.atol_p, c.prm.rtol_p, c.prm.maxiter, c.stats + 1, stream);
             if (rc) return rc;
             if (last) mark(3);
             // :144-147

@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
         sc.rr = red[0];
         sc.rr0 = red[0];
         sc.bb = red[1];
-        sc.thr2 = a.atol2;
+        sc.thr2 = fmax(a.atol2, a.rtol2 * red[0]);
         sc.rho = red[0];
         sc.bf = 0.0f;  // the first direction is r itself
         sc.of = 0.0f;

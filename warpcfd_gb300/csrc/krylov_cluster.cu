@@ -193,6 +193,7 @@ __global__ void __launch_bounds__(CBS) cg_cluster_batched(const wcfd_case* __res
     a.A = c.pres;
     a.x = c.p_x;
     a.atol2 = c.prm.atol_p * c.prm.atol_p;
+    a.rtol2 = c.prm.rtol_p * c.prm.rtol_p;
     a.maxiter = c.prm.maxiter;
     a.stats = c.stats + 1;
     cg_cluster_body<W>(a, (c.mesh.n_cells + cs - 1) / cs);
@@ -208,7 +209,7 @@ template <int W>
 __global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case* __restrict__ cases, int cs_req) {
     __shared__ ff slots[2 * 3 * 16];
     struct Scal {
-        double rr, rho, alpha, rr0, bb;
+        double rr, rho, alpha, rr0, bb, thr2;
         float af, bf, of;
         int go, status, k;
     };
@@ -232,6 +233,7 @@ __global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case*
     const int* __restrict__ col = cse.mesh.ell_col;
     float* x = cse.hbya;
     const double atol2 = cse.prm.atol_u * cse.prm.atol_u;
+    const double rtol2 = cse.prm.rtol_u * cse.prm.rtol_u;
     const int maxiter = cse.prm.maxiter;
     const int stride = (int)cs * CBS;
     const int i0 = (int)me * CBS + threadIdx.x;
@@ -270,11 +272,12 @@ __global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case*
         sc.rr0 = red[0];
         sc.bb = red[1];
         sc.rho = red[0];
+        sc.thr2 = fmax(atol2, rtol2 * red[0]);
         sc.bf = 0.0f;
         sc.of = 0.0f;
         sc.k = 0;
         sc.status = WCFD_OK;
-        sc.go = (0 < maxiter && red[0] > atol2);
+        sc.go = (0 < maxiter && red[0] > sc.thr2);
     }
     __syncthreads();
     int cur = 0;
@@ -389,7 +392,7 @@ __global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case*
             } else {
                 sc.bf = (float)((rr2[1] / sc.rho) * (sc.alpha / omega));
                 sc.rho = rr2[1];
-                sc.go = (sc.k < maxiter && sc.rr > atol2);
+                sc.go = (sc.k < maxiter && sc.rr > sc.thr2);
             }
         }
         __syncthreads();
@@ -397,7 +400,7 @@ __global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case*
     }
     if (me == 0 && threadIdx.x == 0) {
         int st = sc.status;
-        if (st == WCFD_OK && !(sc.rr <= atol2)) st = WCFD_NOT_CONVERGED;
+        if (st == WCFD_OK && !(sc.rr <= sc.thr2)) st = WCFD_NOT_CONVERGED;
         cse.stats[0].iterations = sc.k;
         cse.stats[0].status = st;
         cse.stats[0].residual = sqrt(sc.rr);

@@ -62,6 +62,13 @@ class Result:
     def latency(self):
         return self.finished - self.arrival
 
+    @property
+    def status(self):
+        """converged, diverged (non-finite residual) or exhausted (max_outer reached)."""
+        if self.converged:
+            return "converged"
+        return "exhausted" if math.isfinite(self.residual) else "diverged"
+
 
 def side_ladder(lo=32, hi=256, steps=28):
     """Log-spaced cavity side lengths (cells) from lo to hi."""
@@ -104,8 +111,26 @@ class MeshCache:
         return self.meshes[key]
 
 
-def build_solver(req: Request, mesh, atol=1e-8, maxiter=500, device=None):
-    """FVM + SIMPLE solver of one request (relaxation 0.7 / 0.3, nu = speed * L / Re)."""
+RELAXATION = {
+    # (u, p): the relaxation of the reference's own examples for each kind
+    # (examples/LDC/LDC.py:48 and examples/Channel Flow/Channel Flow.py:51); the reference
+    # method diverges on channels at the cavity's 0.7 / 0.3
+    "cavity": (0.7, 0.3),
+    "channel": (0.3, 0.3),
+}
+
+
+# Krylov stops of the served cases: each solve ends when its residual has dropped tenfold
+# (or below 1e-12), so solve accuracy follows the outer residual down to the 1e-6 target;
+# a fixed atol either stalls the outer iteration at its own level (1e-8: ~2e-6) or costs
+# 3-4x the Krylov iterations (1e-10) for the same outer convergence.
+SERVE_ATOL = 1e-12
+SERVE_RTOL = (0.1, 0.1)
+
+
+def build_solver(req: Request, mesh, atol=1e-8, maxiter=500, device=None, rtol=(0.0, 0.0)):
+    """FVM + SIMPLE solver of one request (relaxation by kind, nu = speed * L / Re).
+    ``rtol`` = (momentum, pressure) relative Krylov stops on top of ``atol``."""
     nu = req.speed * 1.0 / req.re
     model = FVM(mesh, device=device)
     model.material.create_incompressible_newtonian_fluid(viscosity=nu, density=1.0)
@@ -124,10 +149,11 @@ def build_solver(req: Request, mesh, atol=1e-8, maxiter=500, device=None):
     b.slip_wall("-Z")
     b.slip_wall("+Z")
     model.finalize()
-    solver = IncompressibleSolver(model, 0.7, 0.3)
+    solver = IncompressibleSolver(model, *RELAXATION[req.kind])
     solver.verbose = False
     solver.vel_equation.tol = atol
     solver.p_corr_equation.tol = atol
+    solver.vel_equation.rtol, solver.p_corr_equation.rtol = rtol
     solver.vel_equation.max_iter = maxiter
     solver.p_corr_equation.max_iter = maxiter
     return model, solver
@@ -170,9 +196,15 @@ class ServeReport:
 
     def summary(self):
         lat = np.array([r.latency for r in self.results]) if self.results else np.zeros(1)
+        conv = [r for r in self.results if r.converged]
+        lat_c = np.array([r.latency for r in conv]) if conv else np.full(1, np.nan)
         return {
             "requests": len(self.results),
-            "converged": int(sum(r.converged for r in self.results)),
+            "converged": len(conv),
+            "diverged": int(sum(r.status == "diverged" for r in self.results)),
+            "exhausted": int(sum(r.status == "exhausted" for r in self.results)),
+            "p50_converged_s": float(np.percentile(lat_c, 50)),
+            "p99_converged_s": float(np.percentile(lat_c, 99)),
             "p50_s": float(np.percentile(lat, 50)),
             "p99_s": float(np.percentile(lat, 99)),
             "cell_iterations_per_s": self.cell_iterations / max(self.wall, 1e-9),
@@ -186,8 +218,8 @@ class Server:
     """Continuous batching over size buckets (bucket = cell count up to its bound)."""
 
     def __init__(self, hbm_budget=16 << 30, max_active=96, tol=1e-6, check_every=10, max_outer=4000,
-                 buckets=(4096, 16384, 65536), atol=1e-8, device=None, clock=time.perf_counter,
-                 keep_fields=False):
+                 buckets=(4096, 16384, 65536), atol=SERVE_ATOL, rtol=SERVE_RTOL, device=None,
+                 clock=time.perf_counter, keep_fields=False):
         self.budget = int(hbm_budget)
         self.max_active = int(max_active)
         self.tol = float(tol)
@@ -195,6 +227,7 @@ class Server:
         self.max_outer = int(max_outer)
         self.bounds = tuple(sorted(buckets))
         self.atol = atol
+        self.rtol = tuple(rtol)
         self.device = device or torch.device("cuda", torch.cuda.current_device())
         self.clock = clock
         self.meshes = MeshCache()
@@ -234,7 +267,7 @@ class Server:
                 if n_active >= self.max_active or used + estimate_bytes(req.cells) > self.budget:
                     break
                 mesh = self.meshes.get(req.kind, req.cells)
-                model, solver = build_solver(req, mesh, atol=self.atol, device=self.device)
+                model, solver = build_solver(req, mesh, atol=self.atol, device=self.device, rtol=self.rtol)
                 nb = case_bytes(model, solver)
                 used += nb
                 report.peak_bytes = max(report.peak_bytes, used)
@@ -273,7 +306,7 @@ class Server:
                     s.iterations += self.check_every
                     report.cell_iterations += s.model.num_cells * self.check_every
                     done = bool(r < self.tol)
-                    if done or s.iterations >= self.max_outer:
+                    if done or not math.isfinite(r) or s.iterations >= self.max_outer:
                         report.results.append(Result(s.req.rid, s.req.kind, s.model.num_cells, s.iterations, done,
                                                      float(r), s.req.arrival, s.admitted, self.clock() - t0,
                                                      s.model.cell_values.clone() if self.keep_fields else None))
@@ -287,7 +320,7 @@ class Server:
         return report
 
 
-def run_drop_in(requests, tol=1e-6, check_every=10, max_outer=4000, atol=1e-8, device=None):
+def run_drop_in(requests, tol=1e-6, check_every=10, max_outer=4000, atol=SERVE_ATOL, rtol=SERVE_RTOL, device=None):
     """The same requests through the plain drop-in path, one case at a time in arrival
     order: the baseline the batched server is compared with."""
     meshes = MeshCache()
@@ -295,7 +328,7 @@ def run_drop_in(requests, tol=1e-6, check_every=10, max_outer=4000, atol=1e-8, d
     t0 = time.perf_counter()
     results = []
     for req in sorted(requests, key=lambda r: r.arrival):
-        model, solver = build_solver(req, meshes.get(req.kind, req.cells), atol=atol, device=device)
+        model, solver = build_solver(req, meshes.get(req.kind, req.cells), atol=atol, device=device, rtol=rtol)
         it = 0
         r = float("inf")
         while it < max_outer:
@@ -304,7 +337,7 @@ def run_drop_in(requests, tol=1e-6, check_every=10, max_outer=4000, atol=1e-8, d
             it += check_every
             st = solver.solve_stats()[0]
             r = st["initial_residual"] / max(st["rhs_norm"], 1e-300)
-            if r < tol:
+            if r < tol or not math.isfinite(r):
                 break
         cell_iters += model.num_cells * it
         results.append((req.rid, it, r))
