@@ -335,6 +335,7 @@ def run_ours(args):
     for _ in range(args.warmup):
         solver.step()
     torch.cuda.synchronize()
+    snap = solver.snapshot()  # the end-to-end pass below replays the same K steps from here
 
     K_ = args.steps
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * K_)]
@@ -376,22 +377,27 @@ def run_ours(args):
         total_ms = float(t.item())
     value = world * C * K_ / (total_ms * 1e-3)
 
-    # end to end through the public API with host buffers (H2D inputs, D2H result per step)
+    # end to end through the public API with host buffers (H2D inputs, D2H result per step):
+    # the same K steps again from the post-warm-up snapshot (the path is bitwise
+    # reproducible, so the Krylov counts match the timed steps one for one)
+    solver.restore(snap)
     host_in = torch.empty((C, 4), dtype=torch.float32).pin_memory()
     host_out = torch.empty((C, 4), dtype=torch.float32).pin_memory()
     host_in.copy_(model.cell_values.cpu())
-    K_e2e = max(1, K_ // 2)
+    e2e_stats = torch.zeros_like(stats_hist)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for i in range(K_e2e):
+    for i in range(K_):
         model.cell_values.copy_(host_in, non_blocking=True)
         solver.step()
+        e2e_stats[i].copy_(solver.stats)
         host_out.copy_(model.cell_values, non_blocking=True)
         torch.cuda.synchronize()
         host_in, host_out = host_out, host_in
     e2e_s = time.perf_counter() - t0
-    e2e = {"value": world * C * K_e2e / e2e_s, "unit": METRIC, "h2d_bytes_per_step": C * 16,
-           "d2h_bytes_per_step": C * 16}
+    same = bool(torch.equal(e2e_stats, stats_hist))
+    e2e = {"value": world * C * K_ / e2e_s, "unit": METRIC, "h2d_bytes_per_step": C * 16,
+           "d2h_bytes_per_step": C * 16, "same_steps_as_timed": same}
 
     # roofline of the dominant kernel (algorithmic bytes / event time)
     cg_bytes = sum(perfmodel.cg_bytes(C, W, int(k)) for k in k_p)

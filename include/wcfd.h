@@ -250,7 +250,7 @@ int wcfd_krylov_solve(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_w
  * hold their input and output device arrays but cannot allocate device workspace (device
  * memory budgeted at start-up, plugins that may not allocate): the Krylov workspace is a
  * fixed array inside the library, sized for at most WCFD_NOALLOC_MAX_CELLS rows (about
- * 2.6 MiB, held by every GPU that loads the library until exit); larger systems return
+ * 3.1 MiB, held by every GPU that loads the library until exit); larger systems return
  * WCFD_ERR_TOO_LARGE.  The first call on a device looks up the array's device address
  * (make it before any stream capture).  The call allocates nothing.  All calls share the
  * array, so calls that overlap on the GPU race; results are those of wcfd_cg. */

@@ -55,7 +55,7 @@ def test_argument_errors_are_status_codes(built_lib):
 
     lib = _lib.load()
     assert lib.wcfd_version() >= 100
-    assert lib.wcfd_krylov_workspace_floats(100, 1) == 500
+    assert lib.wcfd_krylov_workspace_floats(100, 1) == 600
     assert lib.wcfd_krylov_workspace_floats(100, 3) == 2700
     assert lib.wcfd_krylov_workspace_floats(0, 1) == -1
     rc = lib.wcfd_simple_iteration(None, None)

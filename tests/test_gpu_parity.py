@@ -165,6 +165,26 @@ def test_piso_steps_track_oracle():
         assert rel_l2(g[:, 3], oc.cell_values[:, 3]) < 1e-3, it
 
 
+def test_snapshot_restore_replays_steps_bitwise():
+    """Checkpoint/resume of a case: the steps after restore() repeat those after snapshot()."""
+    m = cavity_mesh(24, jitter=0.1, seed=4)
+    model, solver, _ = make_pair(m, cavity_bc, atol=1e-7)
+    for _ in range(3):
+        solver.step()
+    snap = solver.snapshot()
+    for _ in range(4):
+        solver.step()
+    torch.cuda.synchronize()
+    first = model.cell_values.clone()
+    k_first = solver.solve_stats()
+    solver.restore(snap)
+    for _ in range(4):
+        solver.step()
+    torch.cuda.synchronize()
+    assert torch.equal(model.cell_values, first)
+    assert solver.solve_stats() == k_first
+
+
 def test_cuda_graph_replay_is_bitwise_identical():
     m = cavity_mesh(16)
     model_a, solver_a, _ = make_pair(m, cavity_bc)

@@ -134,6 +134,31 @@ class IncompressibleSolver:
                            ve.workspace_struct(), pe.workspace_struct(),
                            self.stats.data_ptr(), self.params(), self._events_ptr)
 
+    # ------------------------------------------------------------------ checkpoint
+    def state_tensors(self):
+        """The device arrays that carry a case from one step to the next: the model's
+        fields and mass fluxes, HbyA (momentum warm start), the pressure solution (warm
+        start), rUA, rUA_f, the divergence and the fp64 pressure of the precision form.
+        Everything else a step touches is rewritten before it is read."""
+        m = self.model
+        ts = [m.cell_values, m.cell_gradients, m.face_values, m.face_gradients, m.mass_fluxes, self.HbyA,
+              self.p_corr_equation.x, self.rUA, self.rUA_faces, self.div_u]
+        if self.p_x64 is not None:
+            ts.append(self.p_x64)
+        return ts
+
+    def snapshot(self):
+        """Device copies of the case state (resume with restore())."""
+        return [t.clone() for t in self.state_tensors()]
+
+    def restore(self, snap):
+        """Put a snapshot() back; the next steps repeat the ones that followed it bit for bit."""
+        ts = self.state_tensors()
+        if len(ts) != len(snap):
+            raise ValueError("snapshot does not match this case")
+        for t, v in zip(ts, snap):
+            t.copy_(v)
+
     # ------------------------------------------------------------------ stepping
     def step(self):
         """One SIMPLE outer iteration or one PISO time step on the current stream."""

@@ -19,9 +19,7 @@ int batch_budget_rows(int W) {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    const long long budget = (long long)optin - 4096;  // static shared memory and reserve
-    const long long r = budget > 0 ? budget / (6LL * W + 28) : 0;
-    return (int)(r < 4096 ? r : 4096);  // 12-bit local index of the packed columns
+    return cluster_cg_max_rows(W, optin);
 }
 
 int pick_cluster(const wcfd_batch_dims& d) {
@@ -35,17 +33,23 @@ int pick_cluster(const wcfd_batch_dims& d) {
 
 int launch_cluster(const void* fn, int n_cases, int cs, size_t smem, cudaStream_t st, void** args) {
     static std::mutex mu;
-    static size_t set_bytes[64] = {0};
-    static const void* set_fn[64] = {nullptr};
+    static size_t set_bytes[128] = {0};
+    static const void* set_fn[128] = {nullptr};
+    static int set_dev[128] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
     {
         std::lock_guard<std::mutex> lk(mu);
         int slot = -1;
-        for (int i = 0; i < 64; ++i)
-            if (set_fn[i] == fn || set_fn[i] == nullptr) {
+        for (int i = 0; i < 128; ++i)
+            if ((set_fn[i] == fn && set_dev[i] == dev) || set_fn[i] == nullptr) {
                 slot = i;
                 break;
             }
-        if (slot < 0) return WCFD_ERR_CUDA;
+        if (slot < 0) {
+            std::snprintf(g_batch_error, sizeof(g_batch_error), "cluster kernel attribute cache full");
+            return WCFD_ERR_CUDA;
+        }
         if (set_fn[slot] == nullptr || set_bytes[slot] < smem) {
             if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
                 cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
@@ -54,6 +58,7 @@ int launch_cluster(const void* fn, int n_cases, int cs, size_t smem, cudaStream_
                 return WCFD_ERR_CUDA;
             }
             set_fn[slot] = fn;
+            set_dev[slot] = dev;
             set_bytes[slot] = smem;
         }
     }
@@ -118,7 +123,7 @@ extern "C" int wcfd_batch_simple_iteration(const wcfd_case* cases, int32_t n_cas
         std::snprintf(g_batch_error, sizeof(g_batch_error), "max_cells %d too large for cluster size %d", d.max_cells, cs);
         return WCFD_ERR_TOO_LARGE;
     }
-    const void* cg_fn = cg_cluster_batched_for(d.ell_width);
+    const void* cg_fn = cg_cluster_batched_for(d.ell_width, R);
     const void* bi_fn = bicgstab_cluster_batched_for(d.ell_width);
     if (!cg_fn || !bi_fn) return WCFD_ERR_ARGUMENT;
     cudaStream_t st = S(stream);

@@ -68,6 +68,7 @@ int coop_capacity(const void* fn, int /*unused*/) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int cap = per_sm * sms;
     if (cap > WCFD_MAX_BLOCKS) cap = WCFD_MAX_BLOCKS;
+    if (cap > kSolverBlock) cap = kSolverBlock;  // grid_sync: one waiting thread per block
     if (n < 64) cache[n++] = Entry{fn, dev, cap};
     return cap;
 }
@@ -123,10 +124,7 @@ int try_cluster_cg(const wcfd_mesh* m, wcfd_system A, float* x, double atol, int
     cudaGetDevice(&dev);
     int optin = 0;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    const long long budget = (long long)optin - 8192;  // static shared memory and reserve
-    if (budget <= 0) return -1;
-    long long rmax = budget / (6LL * W + 28);
-    if (rmax > 4096) rmax = 4096;  // 12-bit local index of the packed columns
+    const int rmax = cluster_cg_max_rows(W, optin);
     int cs = 0, R = 0;
     for (int c = 1; c <= 16; c *= 2) {
         const long long r = (C + c - 1) / c;
@@ -138,20 +136,25 @@ int try_cluster_cg(const wcfd_mesh* m, wcfd_system A, float* x, double atol, int
     }
     if (cs == 0) return -1;
     const size_t smem = cluster_cg_smem_bytes(R, W);
-    const void* fn = cg_cluster_kernel_for(W);
+    const void* fn = cg_cluster_kernel_for(W, R);
     if (!fn) return -1;
     static std::mutex mu;
-    static size_t set_bytes[64][7] = {{0}};
+    struct SetA { const void* fn; int dev; size_t bytes; };
+    static SetA set_attr[128];
+    static int n_set = 0;
     {
         std::lock_guard<std::mutex> lk(mu);
-        if (dev >= 64) return -1;
-        if (set_bytes[dev][W] < smem) {
+        int slot = -1;
+        for (int i = 0; i < n_set; ++i)
+            if (set_attr[i].fn == fn && set_attr[i].dev == dev) slot = i;
+        if (slot < 0 || set_attr[slot].bytes < smem) {
             if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
                 cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
                 cudaGetLastError();
                 return -1;
             }
-            set_bytes[dev][W] = smem;
+            if (slot < 0 && n_set < 128) slot = n_set++;
+            if (slot >= 0) set_attr[slot] = SetA{fn, dev, smem};
         }
     }
     cudaLaunchConfig_t cfg = {};
@@ -218,7 +221,7 @@ const char* wcfd_last_error(void) { return g_last_error; }
 
 int64_t wcfd_krylov_workspace_floats(int32_t n_cells, int32_t ncomp) {
     if (n_cells <= 0 || (ncomp != 1 && ncomp != 3)) return -1;
-    return ncomp == 1 ? 5LL * n_cells : 27LL * n_cells;
+    return ncomp == 1 ? 6LL * n_cells : 27LL * n_cells;
 }
 
 int wcfd_face_pass_flags(const wcfd_mesh* m, wcfd_bc bc, wcfd_state s, uint32_t mask, uint32_t flags,
@@ -467,7 +470,7 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
 // and calls that overlap on the GPU (other streams, other threads) race on it.
 namespace {
 
-constexpr size_t kNoAllocVecBytes = 5ull * WCFD_NOALLOC_MAX_CELLS * sizeof(float);
+constexpr size_t kNoAllocVecBytes = 6ull * WCFD_NOALLOC_MAX_CELLS * sizeof(float);
 constexpr size_t kNoAllocPartialsOff = (kNoAllocVecBytes + 255) / 256 * 256;
 constexpr size_t kNoAllocPartialsBytes = 8ull * WCFD_MAX_BLOCKS * sizeof(double);
 constexpr size_t kNoAllocBarrierOff = kNoAllocPartialsOff + kNoAllocPartialsBytes;

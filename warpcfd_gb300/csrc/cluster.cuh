@@ -118,4 +118,54 @@ __device__ __forceinline__ void cluster_reduce_to_thread0(ff (&acc)[NV], double 
     }
 }
 
+// Sum NV float-float values over the CTAs of the cluster, result (float-float, the same bits
+// in every CTA) in thread 0 only.  The block stage is a shared-memory tree instead of a
+// butterfly in every warp, so that most warps issue one store and wait: every thread
+// stores its values into sbuf [NV][CBS]; threads 0..255 merge four each (t, t+256, t+512,
+// t+768); warp 0 merges eight each (l, l+32, ..., l+224), then by butterfly, and stores the
+// CTA total into slot `me` of every CTA (DSMEM); after the cluster barrier warp 0 merges
+// the cs <= 16 slots in rank order.  One cluster barrier and two __syncthreads; slots
+// [2][NV][16] are double-buffered by `parity`.
+template <int NV>
+__device__ __forceinline__ void cluster_reduce_tree(const ff (&acc)[NV], ff (&out)[NV], ff* sbuf, ff* slots,
+                                                    unsigned parity, unsigned me, unsigned cs) {
+    static_assert(CBS == 1024, "the tree assumes 1024 threads");
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) sbuf[i * CBS + t] = acc[i];
+    __syncthreads();
+    if (t < 256) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            ff x = sbuf[i * CBS + t];
+            ff_merge(x, sbuf[i * CBS + t + 256]);
+            ff_merge(x, sbuf[i * CBS + t + 512]);
+            ff_merge(x, sbuf[i * CBS + t + 768]);
+            sbuf[i * CBS + t] = x;  // only thread t reads or writes position t in this stage
+        }
+    }
+    __syncthreads();
+    if (t < 32) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            ff x = sbuf[i * CBS + t];
+#pragma unroll
+            for (int k = 1; k < 8; ++k) ff_merge(x, sbuf[i * CBS + t + 32 * k]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) ff_shfl_merge(x, o);
+            if ((unsigned)t < cs) st_cluster_v2f32(map_rank(slots + (parity * NV + i) * 16 + me, t), x.hi, x.lo);
+        }
+    }
+    cluster_sync_all();
+    if (t < 32) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            ff y = (unsigned)t < cs ? slots[(parity * NV + i) * 16 + t] : ff_zero();
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) ff_shfl_merge(y, o);
+            if (t == 0) out[i] = y;
+        }
+    }
+}
+
 }  // namespace wcfd

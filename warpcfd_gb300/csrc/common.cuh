@@ -89,6 +89,42 @@ __device__ __forceinline__ void ff_shfl_merge(ff& v, int o) {
 
 __device__ __forceinline__ double ff_to_double(const ff& v) { return (double)v.hi + (double)v.lo; }
 
+// Scalar float-float arithmetic for the Krylov recurrences.  One dependent fp64 operation
+// costs about 64 cycles on GB300 and an fp64 division about 600, against about 5 and 50
+// for fp32, and the thread that forms alpha and beta holds up every other thread of the
+// solve; so alpha = rz / pq, beta = rz' / rz and the stop test are evaluated on the
+// float-float sums directly.
+
+// (hi, lo) with |lo| <= ulp(hi) / 2 (Dekker's fast two-sum; the sums above keep |lo| small)
+__device__ __forceinline__ ff ff_norm(const ff& a) {
+    const float s = __fadd_rn(a.hi, a.lo);
+    return ff{s, __fsub_rn(a.lo, __fsub_rn(s, a.hi))};
+}
+__device__ __forceinline__ ff ff_from_double(double d) {
+    const float h = (float)d;
+    return ff{h, (float)(d - (double)h)};
+}
+// a > b and a <= b for normalised operands (both false when either is NaN, as for fp64)
+__device__ __forceinline__ bool ff_gt(const ff& a, const ff& b) {
+    return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo);
+}
+__device__ __forceinline__ bool ff_le(const ff& a, const ff& b) {
+    return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo);
+}
+// a / b rounded to fp32: a float quotient q1, the remainder a - q1 b formed exactly
+// (TwoProduct; a.hi - q1 b.hi is exact by Sterbenz's lemma), one correction q2; q1 + q2
+// agrees with a / b to about 2^-46 before the final rounding.  b.hi != 0.
+__device__ __forceinline__ float ff_div_to_float(const ff& an, const ff& bn) {
+    const ff a = ff_norm(an), b = ff_norm(bn);
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const float p = __fmul_rn(q1, b.hi);
+    const float e = fmaf(q1, b.hi, -p);
+    const float rh = __fsub_rn(a.hi, p);
+    const float rl = __fsub_rn(__fsub_rn(a.lo, e), __fmul_rn(q1, b.lo));
+    const float q2 = __fdiv_rn(__fadd_rn(rh, rl), b.hi);
+    return __fadd_rn(q1, q2);
+}
+
 // Block total of NV float-float accumulators, still as float-float (the same bits in every
 // thread).  Warps merge by butterfly shuffles, then warp 0 merges the warp totals; no fp64
 // instruction is issued (a full-warp fp64 instruction is expensive on GB300).
@@ -131,16 +167,20 @@ struct GridCtl {
 // Barrier + reduction over all blocks of a cooperative launch, for phase number `phase`
 // (1, 2, 3, ... in every block).  v[] holds this block's float-float totals (from
 // block_reduce_ff); on return out[] holds the grid-wide sums in fp64.  Each block
-// publishes its totals and then its flag with one release store (no atomics); all threads
-// of every block wait for the flags in parallel, then warp 0 merges the totals in a fixed
-// order and one thread converts to fp64, so every block gets the same bits on every run.
-// Totals are double-buffered by phase parity: a block can only overwrite a buffer after
-// every block has passed the phase that read it.  Every wait is bounded: on timeout the
-// block sets *err and returns false.
+// publishes its totals and then its flag with one release store (no atomics).  Thread j
+// of every block waits for block j's flag and then fetches block j's totals into shared
+// memory, so the two L2 round trips are paid once, by all threads in parallel; warp 0
+// then merges the totals in a fixed order from shared memory and one thread converts to
+// fp64, so every block gets the same bits on every run.  Totals are double-buffered by
+// phase parity: a block can only overwrite a buffer after every block has passed the
+// phase that read it.  Every wait is bounded: on timeout the block sets *err and returns
+// false.  Requires gridDim.x <= BS.
 template <int NV, int BS>
 __device__ bool grid_sync(const GridCtl& g, const ff* v, double* out, unsigned phase) {
+    static_assert(BS >= 32, "block too small");
     __shared__ int s_fail;
     __shared__ double s_res[NV > 0 ? NV : 1];
+    __shared__ float2 s_part[NV > 0 ? NV : 1][BS];
     if (threadIdx.x == 0) s_fail = 0;
     float2* pb = reinterpret_cast<float2*>(g.partials) + (size_t)(phase & 1u) * 4 * WCFD_MAX_BLOCKS;
     if constexpr (NV > 0) {
@@ -152,7 +192,8 @@ __device__ bool grid_sync(const GridCtl& g, const ff* v, double* out, unsigned p
     __syncthreads();  // this block's writes of the phase happen before its release
     if (threadIdx.x == 0) st_release(g.flags + blockIdx.x, phase);
     bool ok = true;
-    for (int j = threadIdx.x; j < (int)gridDim.x; j += BS) {
+    const int j = threadIdx.x;
+    if (j < (int)gridDim.x) {
         if ((int)(ld_acquire(g.flags + j) - phase) < 0) {
             const uint64_t t0 = global_ns();
             unsigned spins = 0;
@@ -164,7 +205,12 @@ __device__ bool grid_sync(const GridCtl& g, const ff* v, double* out, unsigned p
                 __nanosleep(32);
             }
         }
-        if (!ok) break;
+        if constexpr (NV > 0) {
+            if (ok) {
+#pragma unroll
+                for (int i = 0; i < NV; ++i) s_part[i][j] = __ldcg(pb + i * WCFD_MAX_BLOCKS + j);
+            }
+        }
     }
     if (!ok) {
         atomicExch(g.err, WCFD_BARRIER_TIMEOUT);
@@ -178,10 +224,7 @@ __device__ bool grid_sync(const GridCtl& g, const ff* v, double* out, unsigned p
 #pragma unroll
             for (int i = 0; i < NV; ++i) {
                 ff x = ff_zero();
-                for (int j = lane; j < (int)gridDim.x; j += 32) {
-                    const float2 t = __ldcg(pb + i * WCFD_MAX_BLOCKS + j);
-                    ff_merge(x, ff{t.x, t.y});
-                }
+                for (int k = lane; k < (int)gridDim.x; k += 32) ff_merge(x, ff{s_part[i][k].x, s_part[i][k].y});
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) ff_shfl_merge(x, o);
                 if (lane == 0) s_res[i] = ff_to_double(x);

@@ -50,10 +50,12 @@ struct KrylovArgs {
 // kernel instantiations for off-diagonal width W (0..6), nullptr otherwise
 const void* cg_kernel_for(int W);
 const void* bicgstab_kernel_for(int W);
-const void* cg_cluster_kernel_for(int W);
-const void* cg_cluster_batched_for(int W);
+const void* cg_cluster_kernel_for(int W, int R);
+const void* cg_cluster_batched_for(int W, int R);
 const void* bicgstab_cluster_batched_for(int W);
 size_t cluster_cg_smem_bytes(int R, int W);
+int cluster_cg_max_rows(int W, int optin);
+int cluster_cg_rpt(int R);
 const void* residual64_kernel_for(int W);
 __global__ void refine_update_kernel(int C, double* x64, const float* d, float* x32);
 

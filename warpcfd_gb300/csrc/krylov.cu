@@ -67,15 +67,23 @@ __device__ void write_stats(const KrylovArgs& a, const KScalars& sc) {
 
 // Jacobi-preconditioned CG on a scalar system, W = off-diagonal width known at compile
 // time so the loads of a row's columns and gathered values are all in flight at once.
-// Workspace: r, pA, pB, q, invd (5 C floats).
+// Workspace: r, pA, pB, q, invd, z (6 C floats).
+//
+// Per iteration: (1) p_new = z + beta p_old for the row and every neighbour, q = A p_new,
+// p.q -- and x += alpha_prev p_old, the previous iteration's solution update, which reads
+// the p_old this pass loads anyway; (2) r -= alpha q, z = r / diag, r.r and r.z.  Each
+// thread takes two rows (i, i + stride) per trip of pass (1) so that twice the column,
+// coefficient and gather loads are in flight: the pass is bound by memory latency, not
+// by bandwidth, at one row per thread.
 template <int W>
-__global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
+__global__ void __launch_bounds__(BS, 3) cg_kernel(KrylovArgs a) {
     __shared__ KScalars sc;
     const int C = a.m.n_cells;
     float* r = a.ws;
     float* pbuf[2] = {a.ws + (size_t)C, a.ws + 2 * (size_t)C};
     float* q = a.ws + 3 * (size_t)C;
     float* invd = a.ws + 4 * (size_t)C;
+    float* z = a.ws + 5 * (size_t)C;
     const float* __restrict__ b = a.A.rhs;
     const float* __restrict__ diag = a.A.diag;
     const float* __restrict__ off = a.A.off;
@@ -100,6 +108,7 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
         const float zi = ri * di;
         r[i] = ri;
         invd[i] = di;
+        z[i] = zi;
         pbuf[0][i] = zi;
         ff_fma(acc[0], ri, ri);
         ff_fma(acc[1], ri, zi);
@@ -114,27 +123,62 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
         sc.thr2 = fmax(a.atol2, a.rtol2 * red[0]);
         sc.rz = red[1];
         sc.bf = 0.0f;  // the first direction is z itself
+        sc.af = 0.0f;
         sc.go = (0 < a.maxiter && red[0] > sc.thr2);
     }
     __syncthreads();
     int cur = 0;
+    float pending = 0.0f;  // alpha of the last completed iteration, not yet added to x
     while (sc.go) {
         const float bf = sc.bf;
+        const float ap = pending;
         const float* po = pbuf[cur];  // written by other blocks in this launch: no restrict
         float* pn = pbuf[cur ^ 1];
-        // p_new = z + beta p_old (here and for every neighbour) ; q = A p_new ; p.q
+        // x += alpha_prev p_old ; p_new = z + beta p_old (row and neighbours) ; q = A p_new ; p.q
         ff accq[1] = {ff_zero()};
-        for (int i = i0; i < C; i += stride) {
-            const float pi = r[i] * invd[i] + bf * po[i];
-            float qi = diag[i] * pi;
+        for (int i = i0; i < C; i += 2 * stride) {
+            const int i2 = i + stride;
+            const bool two = i2 < C;
+            const int k2 = two ? i2 : i;  // a lone last row loads itself twice, stores once
+            constexpr int WA = W > 0 ? W : 1;  // no zero-length arrays for W = 0
+            int c1[WA], c2[WA];
+            float o1[WA], o2[WA];
 #pragma unroll
             for (int j = 0; j < W; ++j) {
-                const int c = col[(size_t)j * C + i];
-                qi += off[(size_t)j * C + i] * (r[c] * invd[c] + bf * po[c]);
+                c1[j] = col[(size_t)j * C + i];
+                c2[j] = col[(size_t)j * C + k2];
             }
-            pn[i] = pi;
-            q[i] = qi;
-            ff_fma(accq[0], pi, qi);
+#pragma unroll
+            for (int j = 0; j < W; ++j) {
+                o1[j] = off[(size_t)j * C + i];
+                o2[j] = off[(size_t)j * C + k2];
+            }
+            const float po1 = po[i], po2 = po[k2];
+            const float p1 = z[i] + bf * po1;
+            const float p2 = z[k2] + bf * po2;
+            float q1 = diag[i] * p1;
+            float q2 = diag[k2] * p2;
+            float g1[WA], g2[WA];
+#pragma unroll
+            for (int j = 0; j < W; ++j) {
+                g1[j] = z[c1[j]] + bf * po[c1[j]];
+                g2[j] = z[c2[j]] + bf * po[c2[j]];
+            }
+#pragma unroll
+            for (int j = 0; j < W; ++j) {
+                q1 += o1[j] * g1[j];
+                q2 += o2[j] * g2[j];
+            }
+            if (ap != 0.0f) x[i] += ap * po1;
+            pn[i] = p1;
+            q[i] = q1;
+            ff_fma(accq[0], p1, q1);
+            if (two) {
+                if (ap != 0.0f) x[i2] += ap * po2;
+                pn[i2] = p2;
+                q[i2] = q2;
+                ff_fma(accq[0], p2, q2);
+            }
         }
         double pq[1];
         SYNC(1, accq, pq);
@@ -147,15 +191,16 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
             }
         }
         __syncthreads();
+        pending = 0.0f;  // alpha_prev p_old is in x now
         if (!sc.go) break;
         const float af = sc.af;
-        // x += alpha p ; r -= alpha q ; rr ; rz
+        // r -= alpha q ; z = M r ; rr ; rz
         ff acc2[2] = {ff_zero(), ff_zero()};
         for (int i = i0; i < C; i += stride) {
-            x[i] += af * pn[i];
             const float ri = r[i] - af * q[i];
             r[i] = ri;
             const float zi = ri * invd[i];
+            z[i] = zi;
             ff_fma(acc2[0], ri, ri);
             ff_fma(acc2[1], ri, zi);
         }
@@ -169,7 +214,13 @@ __global__ void __launch_bounds__(BS) cg_kernel(KrylovArgs a) {
             sc.go = (sc.k < a.maxiter && sc.rr > sc.thr2);
         }
         __syncthreads();
+        pending = af;
         cur ^= 1;
+    }
+    // the last iteration's x += alpha p (its p is pbuf[cur] after the swap)
+    if (pending != 0.0f) {
+        const float* pl = pbuf[cur];
+        for (int i = i0; i < C; i += stride) x[i] += pending * pl[i];
     }
     write_stats(a, sc);
 }

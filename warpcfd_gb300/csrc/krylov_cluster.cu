@@ -22,18 +22,33 @@
 
 namespace wcfd {
 
-// dynamic shared memory per CTA for R rows and width W: off (4 W), 16-bit packed columns
-// (2 W), diag, invd, r, z, p (two buffers), q (28).  x stays in global memory (own rows,
-// coalesced).  R <= 4096, so 16 CTAs hold 65536 rows of width 4.
-size_t cluster_cg_smem_bytes(int R, int W) { return (size_t)R * (6 * (size_t)W + 28); }
+// Dynamic shared memory per CTA for R rows and width W: the reduction tree (3 x 1024
+// float-float values), then off (4 W), diag, invd, z, p (two buffers) (20) and 16-bit
+// packed columns (2 W) per row.  x, r and q live in registers (each thread owns the same
+// rows for the whole solve).  16 CTAs of R <= 4096 rows hold 65536 rows of width 4.
+size_t cluster_cg_smem_bytes(int R, int W) {
+    return 3 * (size_t)CBS * sizeof(ff) + (size_t)R * (6 * (size_t)W + 20);
+}
 
-template <int W>
+// largest R whose shared memory fits `optin` bytes per CTA (capped by the 12-bit local
+// index of the packed columns)
+int cluster_cg_max_rows(int W, int optin) {
+    const long long fixed = 3LL * CBS * (long long)sizeof(ff) + 4096;  // tree + static shared memory
+    long long r = ((long long)optin - fixed) / (6LL * W + 20);
+    if (r > 4096) r = 4096;
+    return r > 0 ? (int)r : 0;
+}
+
+// rows per thread for R rows per CTA
+int cluster_cg_rpt(int R) { return R <= CBS ? 1 : (R <= 2 * CBS ? 2 : 4); }
+
+template <int W, int RPT>
 __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
+    constexpr int WA = W > 0 ? W : 1;
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ ff wsum[2 * 3 * 32];
     __shared__ ff slots[2 * 3 * 16];
     struct Scal {
-        double rr, rz, rr0, bb, thr2;
+        ff rr, rz, pq, thr2;
         float af, bf;
         int go, status, k;
     };
@@ -43,19 +58,18 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
     const unsigned cs = cluster_nranks();
     const int row0 = (int)me * R;
     const int nloc = max(0, min(R, C - row0));
-    float* off = reinterpret_cast<float*>(smem);                          // [W][R]
+    ff* sbuf = reinterpret_cast<ff*>(smem);                               // [3][CBS]
+    float* off = reinterpret_cast<float*>(sbuf + 3 * CBS);                // [W][R]
     float* diag = off + (size_t)W * R;
     float* invd = diag + R;
-    float* r = invd + R;
-    float* z = r + R;
+    float* z = invd + R;
     float* pbuf0 = z + R;
     float* pbuf1 = pbuf0 + R;
-    float* q = pbuf1 + R;
-    uint16_t* colp = reinterpret_cast<uint16_t*>(q + R);                // [W][R] (rank << 12) | local
-    float* x = a.x + row0;                                                // global, own rows
+    uint16_t* colp = reinterpret_cast<uint16_t*>(pbuf1 + R);            // [W][R] (rank << 12) | local
+    const int t0 = threadIdx.x;
 
-    // load this CTA's slice of the matrix
-    for (int l = threadIdx.x; l < nloc; l += CBS) {
+    // this CTA's slice of the matrix
+    for (int l = t0; l < nloc; l += CBS) {
         const int g = row0 + l;
         const float d = a.A.diag[g];
         diag[l] = d;
@@ -68,36 +82,51 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
             colp[(size_t)j * R + l] = (uint16_t)((rk << 12) | (c - rk * R));
         }
     }
+    // own rows l = t0 + u CBS, u < RPT: x, r, q in registers
+    float xr[RPT], rr_[RPT], qr[RPT], pr[RPT];
     // r = b - A x (x read from global) ; z = M r ; p = z ; rr ; rz ; bb
     ff acc[3] = {ff_zero(), ff_zero(), ff_zero()};
-    for (int l = threadIdx.x; l < nloc; l += CBS) {
-        float ax = diag[l] * x[l];
 #pragma unroll
-        for (int j = 0; j < W; ++j) ax += off[(size_t)j * R + l] * a.x[a.m.ell_col[(size_t)j * C + row0 + l]];
-        const float bi = a.A.rhs[row0 + l];
-        const float ri = bi - ax;
-        const float zi = ri * invd[l];
-        r[l] = ri;
-        z[l] = zi;
-        pbuf0[l] = zi;
-        ff_fma(acc[0], ri, ri);
-        ff_fma(acc[1], ri, zi);
-        ff_fma(acc[2], bi, bi);
+    for (int u = 0; u < RPT; ++u) {
+        const int l = t0 + u * CBS;
+        xr[u] = 0.0f;
+        rr_[u] = 0.0f;
+        qr[u] = 0.0f;
+        pr[u] = 0.0f;
+        if (l < nloc) {
+            const int g = row0 + l;
+            xr[u] = a.x[g];
+            float ax = diag[l] * xr[u];
+#pragma unroll
+            for (int j = 0; j < W; ++j) ax += off[(size_t)j * R + l] * a.x[a.m.ell_col[(size_t)j * C + g]];
+            const float bi = a.A.rhs[g];
+            const float ri = bi - ax;
+            const float zi = ri * invd[l];
+            rr_[u] = ri;
+            z[l] = zi;
+            pbuf0[l] = zi;
+            ff_fma(acc[0], ri, ri);
+            ff_fma(acc[1], ri, zi);
+            ff_fma(acc[2], bi, bi);
+        }
     }
     unsigned parity = 0;
-    double red[3];
-    cluster_reduce_to_thread0<3>(acc, red, wsum, slots, parity, me, cs);
+    ff red[3];
+    cluster_reduce_tree<3>(acc, red, sbuf, slots, parity, me, cs);
     parity ^= 1u;
-    if (threadIdx.x == 0) {
-        sc.rr = red[0];
-        sc.rr0 = red[0];
-        sc.bb = red[2];
-        sc.thr2 = fmax(a.atol2, a.rtol2 * red[0]);
-        sc.rz = red[1];
+    if (t0 == 0) {
+        const double rr0 = ff_to_double(red[0]);
+        sc.rr = ff_norm(red[0]);
+        sc.rz = ff_norm(red[1]);
+        sc.thr2 = ff_norm(ff_from_double(fmax(a.atol2, a.rtol2 * rr0)));
         sc.bf = 0.0f;
         sc.k = 0;
         sc.status = WCFD_OK;
-        sc.go = (0 < a.maxiter && red[0] > sc.thr2);
+        sc.go = (0 < a.maxiter && ff_gt(sc.rr, sc.thr2));
+        if (me == 0) {
+            a.stats->initial_residual = sqrt(rr0);
+            a.stats->rhs_norm = sqrt(ff_to_double(red[2]));
+        }
     }
     __syncthreads();
     int cur = 0;
@@ -105,39 +134,47 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
         const float bf = sc.bf;
         const float* po = cur ? pbuf1 : pbuf0;
         float* pn = cur ? pbuf0 : pbuf1;
-        // p = z + beta p_old (here and for each neighbour) ; q = A p ; p.q
+        // p = z + beta p_old (own row and each neighbour) ; q = A p ; p.q
         ff accq[1] = {ff_zero()};
-        for (int l = threadIdx.x; l < nloc; l += CBS) {
-            const float pi = z[l] + bf * po[l];
-            float qi = diag[l] * pi;
 #pragma unroll
-            for (int j = 0; j < W; ++j) {
-                const unsigned cp = colp[(size_t)j * R + l];
-                const unsigned rk = cp >> 12;
-                const unsigned lo = cp & 0xFFFu;
-                float zc, pc;
-                if (rk == me) {
-                    zc = z[lo];
-                    pc = po[lo];
-                } else {
-                    zc = ld_cluster_f32(map_rank(z + lo, rk));
-                    pc = ld_cluster_f32(map_rank(po + lo, rk));
+        for (int u = 0; u < RPT; ++u) {
+            const int l = t0 + u * CBS;
+            if (l < nloc) {
+                const float pi = z[l] + bf * po[l];
+                float qi = diag[l] * pi;
+                unsigned cp[WA];
+#pragma unroll
+                for (int j = 0; j < W; ++j) cp[j] = colp[(size_t)j * R + l];
+#pragma unroll
+                for (int j = 0; j < W; ++j) {
+                    const unsigned rk = cp[j] >> 12;
+                    const unsigned lo = cp[j] & 0xFFFu;
+                    float zc, pc;
+                    if (rk == me) {
+                        zc = z[lo];
+                        pc = po[lo];
+                    } else {
+                        zc = ld_cluster_f32(map_rank(z + lo, rk));
+                        pc = ld_cluster_f32(map_rank(po + lo, rk));
+                    }
+                    qi += off[(size_t)j * R + l] * (zc + bf * pc);
                 }
-                qi += off[(size_t)j * R + l] * (zc + bf * pc);
+                pn[l] = pi;
+                pr[u] = pi;
+                qr[u] = qi;
+                ff_fma(accq[0], pi, qi);
             }
-            pn[l] = pi;
-            q[l] = qi;
-            ff_fma(accq[0], pi, qi);
         }
-        double pq[1];
-        cluster_reduce_to_thread0<1>(accq, pq, wsum, slots, parity, me, cs);
+        ff pq[1];
+        cluster_reduce_tree<1>(accq, pq, sbuf, slots, parity, me, cs);
         parity ^= 1u;
-        if (threadIdx.x == 0) {
-            if (pq[0] == 0.0) {
+        if (t0 == 0) {
+            const ff pqn = ff_norm(pq[0]);
+            if (pqn.hi == 0.0f) {
                 sc.status = WCFD_KRYLOV_BREAKDOWN;
                 sc.go = 0;
             } else {
-                sc.af = (float)(sc.rz / pq[0]);
+                sc.af = ff_div_to_float(sc.rz, pqn);
             }
         }
         __syncthreads();
@@ -145,47 +182,55 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
         const float af = sc.af;
         // x += alpha p ; r -= alpha q ; z = M r ; rr ; rz
         ff acc2[2] = {ff_zero(), ff_zero()};
-        for (int l = threadIdx.x; l < nloc; l += CBS) {
-            x[l] += af * pn[l];
-            const float ri = r[l] - af * q[l];
-            const float zi = ri * invd[l];
-            r[l] = ri;
-            z[l] = zi;
-            ff_fma(acc2[0], ri, ri);
-            ff_fma(acc2[1], ri, zi);
+#pragma unroll
+        for (int u = 0; u < RPT; ++u) {
+            const int l = t0 + u * CBS;
+            if (l < nloc) {
+                xr[u] += af * pr[u];
+                const float ri = rr_[u] - af * qr[u];
+                const float zi = ri * invd[l];
+                rr_[u] = ri;
+                z[l] = zi;
+                ff_fma(acc2[0], ri, ri);
+                ff_fma(acc2[1], ri, zi);
+            }
         }
-        double red2[2];
-        cluster_reduce_to_thread0<2>(acc2, red2, wsum, slots, parity, me, cs);
+        ff red2[2];
+        cluster_reduce_tree<2>(acc2, red2, sbuf, slots, parity, me, cs);
         parity ^= 1u;
-        if (threadIdx.x == 0) {
-            sc.rr = red2[0];
-            sc.bf = (float)(sc.rz != 0.0 ? red2[1] / sc.rz : 0.0);
-            sc.rz = red2[1];
+        if (t0 == 0) {
+            const ff rzn = ff_norm(red2[1]);
+            sc.rr = ff_norm(red2[0]);
+            sc.bf = sc.rz.hi != 0.0f ? ff_div_to_float(rzn, sc.rz) : 0.0f;
+            sc.rz = rzn;
             sc.k += 1;
-            sc.go = (sc.k < a.maxiter && sc.rr > sc.thr2);
+            sc.go = (sc.k < a.maxiter && ff_gt(sc.rr, sc.thr2));
         }
         __syncthreads();
         cur ^= 1;
     }
-    if (me == 0 && threadIdx.x == 0) {
+#pragma unroll
+    for (int u = 0; u < RPT; ++u) {
+        const int l = t0 + u * CBS;
+        if (l < nloc) a.x[row0 + l] = xr[u];
+    }
+    if (me == 0 && t0 == 0) {
         int st = sc.status;
-        if (st == WCFD_OK && !(sc.rr <= sc.thr2)) st = WCFD_NOT_CONVERGED;
+        if (st == WCFD_OK && !ff_le(sc.rr, sc.thr2)) st = WCFD_NOT_CONVERGED;
         a.stats->iterations = sc.k;
         a.stats->status = st;
-        a.stats->residual = sqrt(sc.rr);
-        a.stats->initial_residual = sqrt(sc.rr0);
-        a.stats->rhs_norm = sqrt(sc.bb);
+        a.stats->residual = sqrt(ff_to_double(sc.rr));
     }
 }
 
-template <int W>
+template <int W, int RPT>
 __global__ void __launch_bounds__(CBS) cg_cluster_kernel(KrylovArgs a, int R) {
-    cg_cluster_body<W>(a, R);
+    cg_cluster_body<W, RPT>(a, R);
 }
 
 // One cluster per case of a device case table: the pressure CG of every case
 // (pres system, p_x warm start, stats[1]), cs CTAs per cluster.
-template <int W>
+template <int W, int RPT>
 __global__ void __launch_bounds__(CBS) cg_cluster_batched(const wcfd_case* __restrict__ cases, int cs) {
     const wcfd_case& c = cases[blockIdx.x / cs];
     KrylovArgs a = {};
@@ -196,7 +241,7 @@ __global__ void __launch_bounds__(CBS) cg_cluster_batched(const wcfd_case* __res
     a.rtol2 = c.prm.rtol_p * c.prm.rtol_p;
     a.maxiter = c.prm.maxiter;
     a.stats = c.stats + 1;
-    cg_cluster_body<W>(a, (c.mesh.n_cells + cs - 1) / cs);
+    cg_cluster_body<W, RPT>(a, (c.mesh.n_cells + cs - 1) / cs);
 }
 
 // BiCGSTAB on one case per cluster, for the batched form: the momentum system of the
@@ -421,20 +466,34 @@ __global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case*
         default: return nullptr;                 \
     }
 
-const void* cg_cluster_batched_for(int W) { WCFD_W_SWITCH(cg_cluster_batched) }
-const void* bicgstab_cluster_batched_for(int W) { WCFD_W_SWITCH(bicgstab_cluster_batched) }
-
-const void* cg_cluster_kernel_for(int W) {
-    switch (W) {
-        case 0: return (const void*)cg_cluster_kernel<0>;
-        case 1: return (const void*)cg_cluster_kernel<1>;
-        case 2: return (const void*)cg_cluster_kernel<2>;
-        case 3: return (const void*)cg_cluster_kernel<3>;
-        case 4: return (const void*)cg_cluster_kernel<4>;
-        case 5: return (const void*)cg_cluster_kernel<5>;
-        case 6: return (const void*)cg_cluster_kernel<6>;
-        default: return nullptr;
+#define WCFD_WR_SWITCH(NAME)                                   \
+    switch (W * 8 + cluster_cg_rpt(R)) {                       \
+        case 0 * 8 + 1: return (const void*)NAME<0, 1>;        \
+        case 0 * 8 + 2: return (const void*)NAME<0, 2>;        \
+        case 0 * 8 + 4: return (const void*)NAME<0, 4>;        \
+        case 1 * 8 + 1: return (const void*)NAME<1, 1>;        \
+        case 1 * 8 + 2: return (const void*)NAME<1, 2>;        \
+        case 1 * 8 + 4: return (const void*)NAME<1, 4>;        \
+        case 2 * 8 + 1: return (const void*)NAME<2, 1>;        \
+        case 2 * 8 + 2: return (const void*)NAME<2, 2>;        \
+        case 2 * 8 + 4: return (const void*)NAME<2, 4>;        \
+        case 3 * 8 + 1: return (const void*)NAME<3, 1>;        \
+        case 3 * 8 + 2: return (const void*)NAME<3, 2>;        \
+        case 3 * 8 + 4: return (const void*)NAME<3, 4>;        \
+        case 4 * 8 + 1: return (const void*)NAME<4, 1>;        \
+        case 4 * 8 + 2: return (const void*)NAME<4, 2>;        \
+        case 4 * 8 + 4: return (const void*)NAME<4, 4>;        \
+        case 5 * 8 + 1: return (const void*)NAME<5, 1>;        \
+        case 5 * 8 + 2: return (const void*)NAME<5, 2>;        \
+        case 5 * 8 + 4: return (const void*)NAME<5, 4>;        \
+        case 6 * 8 + 1: return (const void*)NAME<6, 1>;        \
+        case 6 * 8 + 2: return (const void*)NAME<6, 2>;        \
+        case 6 * 8 + 4: return (const void*)NAME<6, 4>;        \
+        default: return nullptr;                               \
     }
-}
+
+const void* cg_cluster_batched_for(int W, int R) { WCFD_WR_SWITCH(cg_cluster_batched) }
+const void* bicgstab_cluster_batched_for(int W) { WCFD_W_SWITCH(bicgstab_cluster_batched) }
+const void* cg_cluster_kernel_for(int W, int R) { WCFD_WR_SWITCH(cg_cluster_kernel) }
 
 }  // namespace wcfd

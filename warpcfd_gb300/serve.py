@@ -193,6 +193,7 @@ class ServeReport:
     cell_iterations: int = 0
     max_active: int = 0
     peak_bytes: int = 0
+    bucket_busy_s: list = field(default_factory=list)
 
     def summary(self):
         lat = np.array([r.latency for r in self.results]) if self.results else np.zeros(1)
@@ -211,6 +212,7 @@ class ServeReport:
             "wall_s": self.wall,
             "max_active": self.max_active,
             "peak_case_bytes": self.peak_bytes,
+            "bucket_gpu_busy_s": [round(x, 3) for x in self.bucket_busy_s],
         }
 
 
@@ -249,74 +251,104 @@ class Server:
                 return i
         return len(self.bounds) - 1
 
+    def _admit(self, req, t0):
+        mesh = self.meshes.get(req.kind, req.cells)
+        model, solver = build_solver(req, mesh, atol=self.atol, device=self.device, rtol=self.rtol)
+        return _Slot(req, model, solver, case_bytes(model, solver), self.clock() - t0)
+
     def run(self, requests) -> ServeReport:
+        """Serve ``requests`` (arrival times relative to the start of the call).
+
+        Each size bucket runs its own rounds of ``check_every`` batched iterations on its own
+        stream, so a bucket of small cases is never held back by a bucket of large ones.  A
+        round ends with an asynchronous copy of the bucket's solver outcomes to pinned host
+        memory; the host polls the round's event, retires converged, diverged and exhausted
+        cases, adds the requests admitted meanwhile and starts the bucket's next round.
+        Admission (mesh lookup, case build and upload) runs on the host while rounds are in
+        flight."""
+        from . import _lib
+
         pending = sorted(requests, key=lambda r: r.arrival)
-        active = [[] for _ in self.bounds]
-        batches = [None for _ in self.bounds]
+        nb = len(self.bounds)
+        active = [[] for _ in range(nb)]     # cases of the bucket's current batch
+        incoming = [[] for _ in range(nb)]   # admitted, joining at the bucket's next round
+        batches = [None] * nb
+        inflight = [None] * nb               # (start event, end event, pinned stats) of the round in flight
+        busy = [0.0] * nb
         used = 0
         report = ServeReport()
+        cur = torch.cuda.current_stream(self.device)
         t0 = self.clock()
         qi = 0
-        while qi < len(pending) or any(active):
+        while qi < len(pending) or any(active) or any(incoming):
+            # admission: arrived requests while slots and memory allow
             now = self.clock() - t0
-            # admit arrived requests while slots and memory allow
-            admitted = False
             while qi < len(pending) and pending[qi].arrival <= now:
-                req = pending[qi]
-                n_active = sum(len(a) for a in active)
-                if n_active >= self.max_active or used + estimate_bytes(req.cells) > self.budget:
+                n_live = sum(len(a) for a in active) + sum(len(a) for a in incoming)
+                if n_live >= self.max_active or used + estimate_bytes(pending[qi].cells) > self.budget:
                     break
-                mesh = self.meshes.get(req.kind, req.cells)
-                model, solver = build_solver(req, mesh, atol=self.atol, device=self.device, rtol=self.rtol)
-                nb = case_bytes(model, solver)
-                used += nb
+                slot = self._admit(pending[qi], t0)
+                used += slot.bytes
                 report.peak_bytes = max(report.peak_bytes, used)
-                bi = self._bucket(model.num_cells)
-                active[bi].append(_Slot(req, model, solver, nb, self.clock() - t0))
-                batches[bi] = None
+                incoming[self._bucket(slot.model.num_cells)].append(slot)
                 qi += 1
-                admitted = True
-            n_active = sum(len(a) for a in active)
-            report.max_active = max(report.max_active, n_active)
-            if n_active == 0:
-                # idle until the next arrival
-                wait = pending[qi].arrival - (self.clock() - t0)
-                if wait > 0:
-                    time.sleep(min(wait, 0.01))
-                continue
-            for bi, slots in enumerate(active):
-                if slots and batches[bi] is None:
-                    batches[bi] = CaseBatch([s.solver for s in slots], cluster_size=self.cluster_sizes[bi])
-            # advance every bucket by check_every outer iterations, buckets overlapping
-            for bi, slots in enumerate(active):
-                if not slots:
+            report.max_active = max(report.max_active, sum(len(a) for a in active) + sum(len(a) for a in incoming))
+            progressed = False
+            for bi in range(nb):
+                if inflight[bi] is not None:
+                    e0, e1, host = inflight[bi]
+                    if not e1.query():
+                        continue
+                    inflight[bi] = None
+                    busy[bi] += e0.elapsed_time(e1) * 1e-3
+                    st = np.frombuffer(host.numpy().tobytes(), dtype=_lib.STATS_DTYPE).reshape(-1, 2)
+                    res = st[:, 0]["initial_residual"] / np.maximum(st[:, 0]["rhs_norm"], 1e-300)
+                    keep = []
+                    for s, r in zip(active[bi], res):
+                        s.iterations += self.check_every
+                        report.cell_iterations += s.model.num_cells * self.check_every
+                        done = bool(r < self.tol)
+                        if done or not math.isfinite(r) or s.iterations >= self.max_outer:
+                            report.results.append(Result(s.req.rid, s.req.kind, s.model.num_cells, s.iterations,
+                                                         done, float(r), s.req.arrival, s.admitted,
+                                                         self.clock() - t0,
+                                                         s.model.cell_values.clone() if self.keep_fields else None))
+                            used -= s.bytes
+                        else:
+                            keep.append(s)
+                    if len(keep) != len(active[bi]):
+                        active[bi] = keep
+                        batches[bi] = None
+                    progressed = True
+                if incoming[bi]:
+                    active[bi].extend(incoming[bi])
+                    incoming[bi] = []
+                    batches[bi] = None
+                if not active[bi]:
                     continue
-                self.streams[bi].wait_stream(torch.cuda.current_stream(self.device))
-                with torch.cuda.stream(self.streams[bi]):
+                if batches[bi] is None:
+                    batches[bi] = CaseBatch([s.solver for s in active[bi]], cluster_size=self.cluster_sizes[bi])
+                stream = self.streams[bi]
+                stream.wait_stream(cur)  # uploads of newly admitted cases
+                host = torch.empty(batches[bi].stats.numel(), dtype=torch.uint8, pin_memory=True)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                with torch.cuda.stream(stream):
+                    e0.record(stream)
                     for _ in range(self.check_every):
                         batches[bi].step()
-            torch.cuda.synchronize(self.device)
-            # retire converged (or exhausted) cases
-            for bi, slots in enumerate(active):
-                if not slots:
-                    continue
-                res = batches[bi].relative_residuals()
-                keep = []
-                for s, r in zip(slots, res):
-                    s.iterations += self.check_every
-                    report.cell_iterations += s.model.num_cells * self.check_every
-                    done = bool(r < self.tol)
-                    if done or not math.isfinite(r) or s.iterations >= self.max_outer:
-                        report.results.append(Result(s.req.rid, s.req.kind, s.model.num_cells, s.iterations, done,
-                                                     float(r), s.req.arrival, s.admitted, self.clock() - t0,
-                                                     s.model.cell_values.clone() if self.keep_fields else None))
-                        used -= s.bytes
-                    else:
-                        keep.append(s)
-                if len(keep) != len(slots):
-                    active[bi] = keep
-                    batches[bi] = None
+                    host.copy_(batches[bi].stats, non_blocking=True)
+                    e1.record(stream)
+                inflight[bi] = (e0, e1, host)
+                progressed = True
+            if not progressed:
+                if not any(active) and not any(incoming) and qi < len(pending):
+                    time.sleep(max(0.0, min(pending[qi].arrival - (self.clock() - t0), 0.01)))
+                else:
+                    time.sleep(20e-6)
+        torch.cuda.synchronize(self.device)
         report.wall = self.clock() - t0
+        report.bucket_busy_s = busy
         return report
 
 
