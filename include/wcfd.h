@@ -283,8 +283,13 @@ typedef struct wcfd_batch_dims {
 } wcfd_batch_dims;
 
 /* Cluster size wcfd_batch_simple_iteration would pick for these dims (0 = no cluster
- * configuration fits: max_cells too large for the cluster-resident CG). */
+ * configuration fits: max_cells too large for the cluster-resident CG).  It prefers at most
+ * 2048 rows per CTA (lower latency per case). */
 int wcfd_batch_cluster_size(const wcfd_batch_dims* dims);
+/* Most rows per CTA the cluster-resident CG holds on the current device for this
+ * off-diagonal width (a cluster of cs CTAs takes cases of up to cs times as many cells;
+ * the fewest CTAs per case give the most cases in flight). */
+int wcfd_batch_max_rows(int32_t ell_width);
 
 /* One SIMPLE outer iteration (or PISO step) of every case in the table
  * (incompressible.py:95-156 for each case). */

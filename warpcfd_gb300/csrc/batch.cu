@@ -96,6 +96,11 @@ int launch_cluster(const void* fn, int n_cases, int cs, size_t smem, cudaStream_
 
 extern "C" const char* wcfd_batch_last_error(void) { return g_batch_error; }
 
+extern "C" int wcfd_batch_max_rows(int32_t ell_width) {
+    if (ell_width < 0 || ell_width > kMaxSlots) return 0;
+    return batch_budget_rows(ell_width);
+}
+
 extern "C" int wcfd_batch_cluster_size(const wcfd_batch_dims* dims) {
     if (!dims || dims->max_cells <= 0 || dims->ell_width < 0 || dims->ell_width > kMaxSlots) return 0;
     return pick_cluster(*dims);

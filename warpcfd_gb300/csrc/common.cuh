@@ -111,6 +111,32 @@ __device__ __forceinline__ bool ff_gt(const ff& a, const ff& b) {
 __device__ __forceinline__ bool ff_le(const ff& a, const ff& b) {
     return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo);
 }
+// a + b of two floats as a normalised float-float (TwoSum)
+__device__ __forceinline__ ff ff_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return ff{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+// a * b in float-float (TwoProduct of the high words plus the cross terms)
+__device__ __forceinline__ ff ff_mul(const ff& a, const ff& b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+    return ff_norm(ff{p, e});
+}
+// a / b in float-float (see ff_div_to_float); b.hi != 0
+__device__ __forceinline__ ff ff_div(const ff& an, const ff& bn) {
+    const ff a = ff_norm(an), b = ff_norm(bn);
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const float p = __fmul_rn(q1, b.hi);
+    const float e = fmaf(q1, b.hi, -p);
+    const float rh = __fsub_rn(a.hi, p);
+    const float rl = __fsub_rn(__fsub_rn(a.lo, e), __fmul_rn(q1, b.lo));
+    const float q2 = __fdiv_rn(__fadd_rn(rh, rl), b.hi);
+    return ff_two_sum(q1, q2);
+}
+__device__ __forceinline__ float ff_to_float(const ff& a) { return __fadd_rn(a.hi, a.lo); }
+
 // a / b rounded to fp32: a float quotient q1, the remainder a - q1 b formed exactly
 // (TwoProduct; a.hi - q1 b.hi is exact by Sterbenz's lemma), one correction q2; q1 + q2
 // agrees with a / b to about 2^-46 before the final rounding.  b.hi != 0.
@@ -166,20 +192,20 @@ struct GridCtl {
 
 // Barrier + reduction over all blocks of a cooperative launch, for phase number `phase`
 // (1, 2, 3, ... in every block).  v[] holds this block's float-float totals (from
-// block_reduce_ff); on return out[] holds the grid-wide sums in fp64.  Each block
+// block_reduce_ff); on return out[] holds the grid-wide sums (normalised float-float).  Each block
 // publishes its totals and then its flag with one release store (no atomics).  Thread j
 // of every block waits for block j's flag and then fetches block j's totals into shared
 // memory, so the two L2 round trips are paid once, by all threads in parallel; warp 0
-// then merges the totals in a fixed order from shared memory and one thread converts to
-// fp64, so every block gets the same bits on every run.  Totals are double-buffered by
+// then merges the totals in a fixed order from shared memory and one thread
+// normalises, so every block gets the same bits on every run.  Totals are double-buffered by
 // phase parity: a block can only overwrite a buffer after every block has passed the
 // phase that read it.  Every wait is bounded: on timeout the block sets *err and returns
 // false.  Requires gridDim.x <= BS.
 template <int NV, int BS>
-__device__ bool grid_sync(const GridCtl& g, const ff* v, double* out, unsigned phase) {
+__device__ bool grid_sync(const GridCtl& g, const ff* v, ff* out, unsigned phase) {
     static_assert(BS >= 32, "block too small");
     __shared__ int s_fail;
-    __shared__ double s_res[NV > 0 ? NV : 1];
+    __shared__ ff s_res[NV > 0 ? NV : 1];
     __shared__ float2 s_part[NV > 0 ? NV : 1][BS];
     if (threadIdx.x == 0) s_fail = 0;
     float2* pb = reinterpret_cast<float2*>(g.partials) + (size_t)(phase & 1u) * 4 * WCFD_MAX_BLOCKS;
@@ -227,7 +253,7 @@ __device__ bool grid_sync(const GridCtl& g, const ff* v, double* out, unsigned p
                 for (int k = lane; k < (int)gridDim.x; k += 32) ff_merge(x, ff{s_part[i][k].x, s_part[i][k].y});
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) ff_shfl_merge(x, o);
-                if (lane == 0) s_res[i] = ff_to_double(x);
+                if (lane == 0) s_res[i] = ff_norm(x);
             }
         }
         __syncthreads();

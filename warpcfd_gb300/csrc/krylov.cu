@@ -1,7 +1,6 @@
 // Persistent Krylov solvers: one cooperative launch per solve, rows distributed
 // grid-stride over all co-resident blocks, fp64-accurate dot products (exact products
-// summed in float-float across threads, warps and blocks and converted to fp64 once;
-// common.cuh) reduced deterministically at bounded grid barriers.  They replace warp.optim.linear.cg /
+// summed in float-float across threads, warps and blocks; common.cuh) reduced deterministically at bounded grid barriers.  They replace warp.optim.linear.cg /
 // bicgstab with the diagonal (Jacobi) preconditioner as called by Equation.solve_Axb
 // (warp_cfd/FV/terms/equation.py:195-200).  Stop test: ||r||_2 <= atol before an
 // iteration, or maxiter iterations.
@@ -12,10 +11,10 @@
 // half of a double buffer.  The arithmetic is the textbook algorithm's, but a CG iteration
 // needs two grid barriers instead of three and a BiCGSTAB iteration three instead of five.
 //
-// All fp64 scalar work (alpha, beta, omega, the stop test) is done by thread 0 of each
-// block and handed to the other threads through shared memory: GB300 runs fp64 at about
-// 1/64 of its fp32 rate, and an fp64 division in every thread would cost more than the
-// memory traffic of the iteration.
+// The scalar recurrences (alpha, beta, omega, the stop test) run on the float-float sums
+// in thread 0 of each block and reach the other threads through shared memory: GB300
+// runs fp64 at about 1/64 of its fp32 rate (a dependent fp64 division costs about 600
+// cycles), and every thread of the grid waits for these few operations.
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -27,7 +26,7 @@ __device__ __forceinline__ float jacobi(float d) { return d != 0.0f ? 1.0f / d :
 
 // Krylov scalars of one block, owned by thread 0
 struct KScalars {
-    double rr, rz, rho, alpha, rr0, bb, thr2;
+    ff rr, rz, rho, alpha, omega, thr2;
     float af, bf, of;
     int go, status, k;
 };
@@ -43,7 +42,7 @@ __device__ void fail_stats(const KrylovArgs& a, int k) {
 }
 
 // block-reduce the float-float accumulators `acc` and sum them over the grid into the
-// fp64 array `out` (NV values)
+// float-float array `out` (NV values)
 #define SYNC(NV, acc, out)                                         \
     do {                                                           \
         block_reduce_ff<NV, BS>(acc);                              \
@@ -53,15 +52,25 @@ __device__ void fail_stats(const KrylovArgs& a, int k) {
         }                                                          \
     } while (0)
 
+// set-up scalars from the initial r.r and b.b; block 0 records ||r_0|| and ||b||
+__device__ void init_scalars(const KrylovArgs& a, KScalars& sc, const ff& rr, const ff& bb) {
+    const double rr0 = ff_to_double(rr);
+    sc.rr = rr;
+    sc.thr2 = ff_norm(ff_from_double(fmax(a.atol2, a.rtol2 * rr0)));
+    sc.go = (0 < a.maxiter && ff_gt(sc.rr, sc.thr2));
+    if (blockIdx.x == 0) {
+        a.stats->initial_residual = sqrt(rr0);
+        a.stats->rhs_norm = sqrt(ff_to_double(bb));
+    }
+}
+
 __device__ void write_stats(const KrylovArgs& a, const KScalars& sc) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         int st = sc.status;
-        if (st == WCFD_OK && !(sc.rr <= sc.thr2)) st = WCFD_NOT_CONVERGED;
+        if (st == WCFD_OK && !ff_le(sc.rr, sc.thr2)) st = WCFD_NOT_CONVERGED;
         a.stats->iterations = sc.k;
         a.stats->status = st;
-        a.stats->residual = sqrt(sc.rr);
-        a.stats->initial_residual = sqrt(sc.rr0);
-        a.stats->rhs_norm = sqrt(sc.bb);
+        a.stats->residual = sqrt(ff_to_double(sc.rr));
     }
 }
 
@@ -114,17 +123,13 @@ __global__ void __launch_bounds__(BS, 3) cg_kernel(KrylovArgs a) {
         ff_fma(acc[1], ri, zi);
         ff_fma(acc[2], b[i], b[i]);
     }
-    double red[3];
+    ff red[3];
     SYNC(3, acc, red);
     if (threadIdx.x == 0) {
-        sc.rr = red[0];
-        sc.rr0 = red[0];
-        sc.bb = red[2];
-        sc.thr2 = fmax(a.atol2, a.rtol2 * red[0]);
+        init_scalars(a, sc, red[0], red[2]);
         sc.rz = red[1];
         sc.bf = 0.0f;  // the first direction is z itself
         sc.af = 0.0f;
-        sc.go = (0 < a.maxiter && red[0] > sc.thr2);
     }
     __syncthreads();
     int cur = 0;
@@ -180,14 +185,14 @@ __global__ void __launch_bounds__(BS, 3) cg_kernel(KrylovArgs a) {
                 ff_fma(accq[0], p2, q2);
             }
         }
-        double pq[1];
+        ff pq[1];
         SYNC(1, accq, pq);
         if (threadIdx.x == 0) {
-            if (pq[0] == 0.0) {
+            if (pq[0].hi == 0.0f) {
                 sc.status = WCFD_KRYLOV_BREAKDOWN;
                 sc.go = 0;
             } else {
-                sc.af = (float)(sc.rz / pq[0]);
+                sc.af = ff_div_to_float(sc.rz, pq[0]);
             }
         }
         __syncthreads();
@@ -204,14 +209,14 @@ __global__ void __launch_bounds__(BS, 3) cg_kernel(KrylovArgs a) {
             ff_fma(acc2[0], ri, ri);
             ff_fma(acc2[1], ri, zi);
         }
-        double red2[2];
+        ff red2[2];
         SYNC(2, acc2, red2);
         if (threadIdx.x == 0) {
             sc.rr = red2[0];
-            sc.bf = (float)(sc.rz != 0.0 ? red2[1] / sc.rz : 0.0);
+            sc.bf = sc.rz.hi != 0.0f ? ff_div_to_float(red2[1], sc.rz) : 0.0f;
             sc.rz = red2[1];
             sc.k += 1;
-            sc.go = (sc.k < a.maxiter && sc.rr > sc.thr2);
+            sc.go = (sc.k < a.maxiter && ff_gt(sc.rr, sc.thr2));
         }
         __syncthreads();
         pending = af;
@@ -279,17 +284,13 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
             ff_fma(acc[1], b[q], b[q]);
         }
     }
-    double red[2];
+    ff red[2];
     SYNC(2, acc, red);
     if (threadIdx.x == 0) {
-        sc.rr = red[0];
-        sc.rr0 = red[0];
-        sc.bb = red[1];
-        sc.thr2 = fmax(a.atol2, a.rtol2 * red[0]);
+        init_scalars(a, sc, red[0], red[1]);
         sc.rho = red[0];
         sc.bf = 0.0f;  // the first direction is r itself
         sc.of = 0.0f;
-        sc.go = (0 < a.maxiter && red[0] > sc.thr2);
     }
     __syncthreads();
     int cur = 0;
@@ -328,15 +329,15 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
                 ff_fma(accv[0], r0[q], vi[o]);
             }
         }
-        double r0v[1];
+        ff r0v[1];
         SYNC(1, accv, r0v);
         if (threadIdx.x == 0) {
-            if (r0v[0] == 0.0) {
+            if (r0v[0].hi == 0.0f) {
                 sc.status = WCFD_KRYLOV_BREAKDOWN;
                 sc.go = 0;
             } else {
-                sc.alpha = sc.rho / r0v[0];
-                sc.af = (float)sc.alpha;
+                sc.alpha = ff_div(sc.rho, r0v[0]);
+                sc.af = ff_to_float(sc.alpha);
             }
         }
         __syncthreads();
@@ -373,9 +374,12 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
                 ff_fma(acct[1], ti[o], si[o]);
             }
         }
-        double ts[2];
+        ff ts[2];
         SYNC(2, acct, ts);
-        if (threadIdx.x == 0) sc.of = (float)(ts[0] != 0.0 ? ts[1] / ts[0] : 0.0);
+        if (threadIdx.x == 0) {
+            sc.omega = ts[0].hi != 0.0f ? ff_div(ts[1], ts[0]) : ff_zero();
+            sc.of = ff_to_float(sc.omega);
+        }
         __syncthreads();
         const float of = sc.of;
         // x += omega M s ; r = s - omega t ; r.r ; r0.r
@@ -392,19 +396,18 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
                 ff_fma(accr[1], r0[q], ri);
             }
         }
-        double rr2[2];
+        ff rr2[2];
         SYNC(2, accr, rr2);
         if (threadIdx.x == 0) {
-            const double omega = ts[0] != 0.0 ? ts[1] / ts[0] : 0.0;
             sc.rr = rr2[0];
             sc.k += 1;
-            if (omega == 0.0 || sc.rho == 0.0) {
+            if (sc.omega.hi == 0.0f || sc.rho.hi == 0.0f) {
                 sc.status = WCFD_KRYLOV_BREAKDOWN;
                 sc.go = 0;
             } else {
-                sc.bf = (float)((rr2[1] / sc.rho) * (sc.alpha / omega));
+                sc.bf = ff_to_float(ff_mul(ff_div(rr2[1], sc.rho), ff_div(sc.alpha, sc.omega)));
                 sc.rho = rr2[1];
-                sc.go = (sc.k < a.maxiter && sc.rr > sc.thr2);
+                sc.go = (sc.k < a.maxiter && ff_gt(sc.rr, sc.thr2));
             }
         }
         __syncthreads();

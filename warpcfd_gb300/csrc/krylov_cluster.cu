@@ -253,8 +253,9 @@ __global__ void __launch_bounds__(CBS) cg_cluster_batched(const wcfd_case* __res
 template <int W>
 __global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case* __restrict__ cases, int cs_req) {
     __shared__ ff slots[2 * 3 * 16];
+    __shared__ ff sbuf[2 * CBS];
     struct Scal {
-        double rr, rho, alpha, rr0, bb, thr2;
+        ff rr, rho, alpha, omega, thr2;
         float af, bf, of;
         int go, status, k;
     };
@@ -309,20 +310,23 @@ __global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case*
             ff_fma(acc[1], b[q], b[q]);
         }
     }
-    double red[2];
-    cluster_allreduce<2>(acc, red, slots, parity, me, cs);
+    ff red[2];
+    cluster_reduce_tree<2>(acc, red, sbuf, slots, parity, me, cs);
     parity ^= 1u;
     if (threadIdx.x == 0) {
-        sc.rr = red[0];
-        sc.rr0 = red[0];
-        sc.bb = red[1];
-        sc.rho = red[0];
-        sc.thr2 = fmax(atol2, rtol2 * red[0]);
+        const double rr0 = ff_to_double(red[0]);
+        sc.rr = ff_norm(red[0]);
+        sc.rho = sc.rr;
+        sc.thr2 = ff_norm(ff_from_double(fmax(atol2, rtol2 * rr0)));
         sc.bf = 0.0f;
         sc.of = 0.0f;
         sc.k = 0;
         sc.status = WCFD_OK;
-        sc.go = (0 < maxiter && red[0] > sc.thr2);
+        sc.go = (0 < maxiter && ff_gt(sc.rr, sc.thr2));
+        if (me == 0) {
+            cse.stats[0].initial_residual = sqrt(rr0);
+            cse.stats[0].rhs_norm = sqrt(ff_to_double(red[1]));
+        }
     }
     __syncthreads();
     int cur = 0;
@@ -360,16 +364,17 @@ __global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case*
                 ff_fma(accv[0], r0[q], vi[o]);
             }
         }
-        double r0v[1];
-        cluster_allreduce<1>(accv, r0v, slots, parity, me, cs);
+        ff r0v[1];
+        cluster_reduce_tree<1>(accv, r0v, sbuf, slots, parity, me, cs);
         parity ^= 1u;
         if (threadIdx.x == 0) {
-            if (r0v[0] == 0.0) {
+            const ff d = ff_norm(r0v[0]);
+            if (d.hi == 0.0f) {
                 sc.status = WCFD_KRYLOV_BREAKDOWN;
                 sc.go = 0;
             } else {
-                sc.alpha = sc.rho / r0v[0];
-                sc.af = (float)sc.alpha;
+                sc.alpha = ff_div(sc.rho, d);
+                sc.af = ff_to_float(sc.alpha);
             }
         }
         __syncthreads();
@@ -405,10 +410,14 @@ __global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case*
                 ff_fma(acct[1], ti[o], si[o]);
             }
         }
-        double ts[2];
-        cluster_allreduce<2>(acct, ts, slots, parity, me, cs);
+        ff ts[2];
+        cluster_reduce_tree<2>(acct, ts, sbuf, slots, parity, me, cs);
         parity ^= 1u;
-        if (threadIdx.x == 0) sc.of = (float)(ts[0] != 0.0 ? ts[1] / ts[0] : 0.0);
+        if (threadIdx.x == 0) {
+            const ff tt = ff_norm(ts[0]);
+            sc.omega = tt.hi != 0.0f ? ff_div(ts[1], tt) : ff_zero();
+            sc.of = ff_to_float(sc.omega);
+        }
         __syncthreads();
         const float of = sc.of;
         ff accr[2] = {ff_zero(), ff_zero()};
@@ -424,20 +433,20 @@ __global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case*
                 ff_fma(accr[1], r0[q], ri);
             }
         }
-        double rr2[2];
-        cluster_allreduce<2>(accr, rr2, slots, parity, me, cs);
+        ff rr2[2];
+        cluster_reduce_tree<2>(accr, rr2, sbuf, slots, parity, me, cs);
         parity ^= 1u;
         if (threadIdx.x == 0) {
-            const double omega = ts[0] != 0.0 ? ts[1] / ts[0] : 0.0;
-            sc.rr = rr2[0];
+            sc.rr = ff_norm(rr2[0]);
             sc.k += 1;
-            if (omega == 0.0 || sc.rho == 0.0) {
+            if (sc.omega.hi == 0.0f || sc.rho.hi == 0.0f) {
                 sc.status = WCFD_KRYLOV_BREAKDOWN;
                 sc.go = 0;
             } else {
-                sc.bf = (float)((rr2[1] / sc.rho) * (sc.alpha / omega));
-                sc.rho = rr2[1];
-                sc.go = (sc.k < maxiter && sc.rr > sc.thr2);
+                const ff rho_n = ff_norm(rr2[1]);
+                sc.bf = ff_to_float(ff_mul(ff_div(rho_n, sc.rho), ff_div(sc.alpha, sc.omega)));
+                sc.rho = rho_n;
+                sc.go = (sc.k < maxiter && ff_gt(sc.rr, sc.thr2));
             }
         }
         __syncthreads();
@@ -445,12 +454,10 @@ __global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case*
     }
     if (me == 0 && threadIdx.x == 0) {
         int st = sc.status;
-        if (st == WCFD_OK && !(sc.rr <= sc.thr2)) st = WCFD_NOT_CONVERGED;
+        if (st == WCFD_OK && !ff_le(sc.rr, sc.thr2)) st = WCFD_NOT_CONVERGED;
         cse.stats[0].iterations = sc.k;
         cse.stats[0].status = st;
-        cse.stats[0].residual = sqrt(sc.rr);
-        cse.stats[0].initial_residual = sqrt(sc.rr0);
-        cse.stats[0].rhs_norm = sqrt(sc.bb);
+        cse.stats[0].residual = sqrt(ff_to_double(sc.rr));
     }
 }
 

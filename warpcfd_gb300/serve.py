@@ -220,7 +220,7 @@ class Server:
     """Continuous batching over size buckets (bucket = cell count up to its bound)."""
 
     def __init__(self, hbm_budget=16 << 30, max_active=96, tol=1e-6, check_every=10, max_outer=4000,
-                 buckets=(4096, 16384, 65536), atol=SERVE_ATOL, rtol=SERVE_RTOL, device=None,
+                 buckets=(4096, 8192, 16384, 32768, 65536), atol=SERVE_ATOL, rtol=SERVE_RTOL, device=None,
                  clock=time.perf_counter, keep_fields=False):
         self.budget = int(hbm_budget)
         self.max_active = int(max_active)
@@ -236,14 +236,21 @@ class Server:
         self.keep_fields = keep_fields
         self.streams = [torch.cuda.Stream(device=self.device) for _ in self.bounds]
         # one cluster size per bucket, from its bound, so a case's arithmetic never depends
-        # on which other cases share its batch
+        # on which other cases share its batch: the fewest CTAs whose shared memory holds
+        # the bucket's largest case (2D-extruded hex meshes: off-diagonal width 4), which
+        # puts the most cases in flight at once
         from . import _lib
-        import ctypes as ct
-        lib = _lib.load()
+        rows = int(_lib.load().wcfd_batch_max_rows(4))
+        if rows <= 0:
+            raise RuntimeError("the cluster-resident solver does not fit this device")
         self.cluster_sizes = []
         for b in self.bounds:
-            d = _lib.BatchDims_t(b, 8 * b, 6, 4, 1, 1, 0, 0)
-            self.cluster_sizes.append(int(lib.wcfd_batch_cluster_size(ct.byref(d))))
+            cs = 1
+            while cs * rows < b:
+                cs *= 2
+            if cs > 16:
+                raise ValueError(f"bucket bound {b} exceeds what 16 CTAs hold ({16 * rows} cells)")
+            self.cluster_sizes.append(cs)
 
     def _bucket(self, cells):
         for i, b in enumerate(self.bounds):
