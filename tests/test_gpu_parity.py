@@ -211,8 +211,11 @@ def test_runs_are_bitwise_reproducible():
 
 @pytest.mark.parametrize("case", ["cavity", "channel", "cavity3d"])
 def test_cg_paths_agree_with_oracle(case):
-    """The cluster-resident CG (shared memory of one thread-block cluster) and the
-    grid-cooperative CG solve the same assembled pressure system like the oracle's CG."""
+    """The cluster-resident CGs (shared memory of one thread-block cluster: textbook, path
+    2, and the single-reduction arrangement, path 3) and the grid-cooperative CG (path 1)
+    solve the same assembled pressure system like the oracle's CG.  The single-reduction
+    iterates equal the textbook ones up to rounding, which on the ill-conditioned channel
+    system moves the solution at the absolute stop by up to ~1e-4: held to 3e-4."""
     import ctypes as ct
 
     from oracle.simple_ref import cg as oracle_cg, jacobi_inverse
@@ -236,7 +239,7 @@ def test_cg_paths_agree_with_oracle(case):
     lib = _lib.load()
     out = {}
     try:
-        for path in (1, 2):
+        for path in (1, 2, 3):
             assert lib.wcfd_set_krylov_path(path) == 0
             x = torch.zeros_like(pe.x)
             pe.tol, pe.max_iter = 1e-6, 300
@@ -246,8 +249,9 @@ def test_cg_paths_agree_with_oracle(case):
         lib.wcfd_set_krylov_path(0)
     for path, (x, st) in out.items():
         assert abs(st["iterations"] - ko) <= max(2, ko // 50), (path, st, ko)
-        assert rel_l2(x, xo) < 1e-4, path
+        assert rel_l2(x, xo) < (1e-4 if path < 3 else 3e-4), path
     assert rel_l2(out[1][0], out[2][0]) < 1e-4
+    assert rel_l2(out[1][0], out[3][0]) < 3e-4
 
 
 def test_cylinder_piso_with_correction_tracks_oracle():
@@ -333,3 +337,43 @@ def test_fp64_refined_pressure_solve_is_fp64_accurate():
     err32 = rel_l2(x_plain.cpu().numpy(), x_exact)
     assert err64 < 1e-9, (err64, err32)
     assert err64 < 1e-3 * err32
+
+
+@pytest.mark.parametrize("path", [1, 2, 3])
+def test_relative_krylov_stop(path):
+    """wcfd_krylov_solve: the solve ends at ||r|| <= rtol ||r_0|| (both methods, both CG
+    paths), after fewer iterations than an absolute stop far below it; rtol 0 reproduces
+    wcfd_cg bit for bit."""
+    from warpcfd_gb300 import _lib
+
+    m = cavity_mesh(24, jitter=0.1, seed=4)
+    model, solver, _ = make_pair(m, cavity_bc)
+    for _ in range(2):
+        solver.step()
+    torch.cuda.synchronize()
+    lib = _lib.load()
+    lib.wcfd_set_krylov_path(path)
+    try:
+        for eq in (solver.p_corr_equation, solver.vel_equation):
+            x0 = eq.x.clone()
+            eq.tol, eq.max_iter, eq.rtol = 1e-14, 500, 1e-2
+            x = x0.clone()
+            st, _ = eq.solve_Axb(x)
+            assert st["residual"] <= 1e-2 * st["initial_residual"] * (1 + 1e-6), st
+            eq.rtol = 1e-6
+            x_deep = x0.clone()
+            deep, _ = eq.solve_Axb(x_deep)
+            assert st["iterations"] < deep["iterations"], (st, deep)
+            # rtol = 0 is the reference's absolute stop: the same bits as wcfd_cg / wcfd_bicgstab
+            eq.rtol, eq.tol = 0.0, 1e-6
+            xa, xb = x0.clone(), x0.clone()
+            sa, _ = eq.solve_Axb(xa)
+            fn = "wcfd_bicgstab" if eq.linear_solver == "bicgstab" else "wcfd_cg"
+            import ctypes as ct
+            _lib.call(fn, ct.byref(model.mesh_struct()), eq.system_struct(), ct.c_void_p(xb.data_ptr()),
+                      eq.workspace_struct(), 1e-6, 500, ct.c_void_p(eq.stats.data_ptr()),
+                      ct.c_void_p(torch.cuda.current_stream().cuda_stream))
+            torch.cuda.synchronize()
+            assert torch.equal(xa, xb)
+    finally:
+        lib.wcfd_set_krylov_path(0)

@@ -112,7 +112,7 @@ int launch_krylov(const void* fn, int slot, const wcfd_mesh* m, wcfd_system A, f
     return WCFD_OK;
 }
 
-int g_krylov_path = 0;  // 0 automatic, 1 grid-cooperative only, 2 cluster-resident when it fits
+int g_krylov_path = 0;  // 0 automatic, 1 grid-cooperative only, 2 cluster-resident when it fits, 3 as 2 with the single-reduction CG
 
 // Cluster-resident CG when the system fits in the shared memory of one cluster of up to
 // 16 CTAs; returns -1 (caller falls back to the grid-cooperative kernel) otherwise.
@@ -135,8 +135,15 @@ int try_cluster_cg(const wcfd_mesh* m, wcfd_system A, float* x, double atol, int
         }
     }
     if (cs == 0) return -1;
-    const size_t smem = cluster_cg_smem_bytes(R, W);
+    // the textbook kernel; the single-reduction arrangement when asked for (path 3) and its
+    // registers (<= 2 rows per thread) and shared memory allow
+    size_t smem = cluster_cg_smem_bytes(R, W);
     const void* fn = cg_cluster_kernel_for(W, R);
+    const size_t smem1 = cluster_cg1_smem_bytes(R, W);
+    if (g_krylov_path == 3 && R <= 2 * kClusterBlock && smem1 + 2048 <= (size_t)optin) {
+        fn = cg1_cluster_kernel_for(W, R);
+        smem = smem1;
+    }
     if (!fn) return -1;
     static std::mutex mu;
     struct SetA { const void* fn; int dev; size_t bytes; };
@@ -171,19 +178,19 @@ int try_cluster_cg(const wcfd_mesh* m, wcfd_system A, float* x, double atol, int
     cfg.numAttrs = 1;
     // whether this (device, size, width) cluster launch is schedulable, asked once
     static std::mutex qmu;
-    struct Q { int dev, C, W, ok; };
-    static Q qcache[32];
+    struct Q { int dev, C; const void* fn; int ok; };
+    static Q qcache[64];
     static int nq = 0;
     int ok = -1;
     {
         std::lock_guard<std::mutex> lk(qmu);
         for (int i = 0; i < nq; ++i)
-            if (qcache[i].dev == dev && qcache[i].C == C && qcache[i].W == W) ok = qcache[i].ok;
+            if (qcache[i].dev == dev && qcache[i].C == C && qcache[i].fn == fn) ok = qcache[i].ok;
         if (ok < 0) {
             int nclusters = 0;
             ok = (cudaOccupancyMaxActiveClusters(&nclusters, fn, &cfg) == cudaSuccess && nclusters >= 1) ? 1 : 0;
             cudaGetLastError();
-            if (nq < 32) qcache[nq++] = Q{dev, C, W, ok};
+            if (nq < 64) qcache[nq++] = Q{dev, C, fn, ok};
         }
     }
     if (!ok) return -1;
@@ -212,7 +219,9 @@ extern "C" {
 int wcfd_version(void) { return 100; }
 
 int wcfd_set_krylov_path(int32_t path) {
-    if (path < 0 || path > 2) return set_error(WCFD_ERR_ARGUMENT, "path must be 0 (auto), 1 (grid), 2 (cluster)");
+    if (path < 0 || path > 3)
+        return set_error(WCFD_ERR_ARGUMENT,
+                         "path must be 0 (auto), 1 (grid), 2 (cluster), 3 (cluster, single-reduction CG)");
     g_krylov_path = path;
     return WCFD_OK;
 }

@@ -56,6 +56,8 @@ const void* bicgstab_cluster_batched_for(int W);
 size_t cluster_cg_smem_bytes(int R, int W);
 int cluster_cg_max_rows(int W, int optin);
 int cluster_cg_rpt(int R);
+const void* cg1_cluster_kernel_for(int W, int R);
+size_t cluster_cg1_smem_bytes(int R, int W);
 const void* residual64_kernel_for(int W);
 __global__ void refine_update_kernel(int C, double* x64, const float* d, float* x32);
 

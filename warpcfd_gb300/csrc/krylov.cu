@@ -78,6 +78,11 @@ __device__ void write_stats(const KrylovArgs& a, const KScalars& sc) {
 // time so the loads of a row's columns and gathered values are all in flight at once.
 // Workspace: r, pA, pB, q, invd, z (6 C floats).
 //
+// The matrix (off-diagonals and columns, 8 W bytes a row) is read with the streaming
+// (evict-first) cache policy: it is re-read every iteration but does not fit L2 next to
+// the vectors on large meshes, and evicting it first keeps the vectors (gathered and
+// re-read within the iteration) resident in the 129 MB L2.
+//
 // Per iteration: (1) p_new = z + beta p_old for the row and every neighbour, q = A p_new,
 // p.q -- and x += alpha_prev p_old, the previous iteration's solution update, which reads
 // the p_old this pass loads anyway; (2) r -= alpha q, z = r / diag, r.r and r.z.  Each
@@ -150,13 +155,13 @@ __global__ void __launch_bounds__(BS, 3) cg_kernel(KrylovArgs a) {
             float o1[WA], o2[WA];
 #pragma unroll
             for (int j = 0; j < W; ++j) {
-                c1[j] = col[(size_t)j * C + i];
-                c2[j] = col[(size_t)j * C + k2];
+                c1[j] = __ldcs(col + (size_t)j * C + i);
+                c2[j] = __ldcs(col + (size_t)j * C + k2);
             }
 #pragma unroll
             for (int j = 0; j < W; ++j) {
-                o1[j] = off[(size_t)j * C + i];
-                o2[j] = off[(size_t)j * C + k2];
+                o1[j] = __ldcs(off + (size_t)j * C + i);
+                o2[j] = __ldcs(off + (size_t)j * C + k2);
             }
             const float po1 = po[i], po2 = po[k2];
             const float p1 = z[i] + bf * po1;

@@ -2,20 +2,24 @@
 // system in shared memory for the length of the solve.
 //
 //  * CTA q of the cluster owns rows [q R, (q+1) R); its slice of the matrix (off-diagonals,
-//    packed (rank, local) columns, diagonal) and of every vector lives in its shared memory.
+//    packed (rank, local) columns, diagonal) and the gathered vectors (z and p, stored as
+//    (z, p) pairs so one 8-byte load fetches both) live in its shared memory; x, r and q of
+//    a thread's own rows stay in registers.
 //  * A neighbour value owned by another CTA is read through distributed shared memory
 //    (mapa + ld.shared::cluster); nothing touches global memory between the set-up and
 //    the final write of x.
 //  * Grid-wide synchronisation is the hardware cluster barrier
-//    (barrier.cluster.arrive.release / wait.acquire).  A dot product is an all-reduce: each
-//    CTA sums its rows (exact products in float-float, common.cuh), stores its fp64 total
-//    into a slot of every CTA's shared memory, and after the barrier one warp per CTA adds
-//    the CS slots in a fixed order, so all CTAs (and all runs) agree bit for bit.  All CTAs take the same branch at every test, so no CTA can
-//    leave while another still waits or reads its memory.
+//    (barrier.cluster.arrive.release / wait.acquire).  A dot product is reduced by a
+//    shared-memory tree in each CTA (exact products in float-float, common.cuh); warp 0
+//    stores the CTA total into a slot of every CTA's shared memory and after the barrier
+//    merges the cs slots in a fixed order, so all CTAs (and all runs) agree bit for bit.
+//    Thread 0 forms alpha and beta from the float-float sums and broadcasts them.  All
+//    CTAs take the same branch at every test, so no CTA can leave while another still
+//    waits or reads its memory.
 //  * The direction update p = z + beta p is evaluated inside the SpMV for the row and its
 //    neighbours (double-buffered p), so an iteration needs two barriers.
 // The arithmetic is that of cg_kernel (krylov.cu): the same Jacobi-preconditioned CG with
-// fp64 dot products and the same stop test.
+// fp64-accurate dot products and the same stop test.
 #include "cluster.cuh"
 #include "common.cuh"
 #include "kernels.cuh"
@@ -23,18 +27,19 @@
 namespace wcfd {
 
 // Dynamic shared memory per CTA for R rows and width W: the reduction tree (3 x 1024
-// float-float values), then off (4 W), diag, invd, z, p (two buffers) (20) and 16-bit
-// packed columns (2 W) per row.  x, r and q live in registers (each thread owns the same
-// rows for the whole solve).  16 CTAs of R <= 4096 rows hold 65536 rows of width 4.
+// float-float values), then per row the pairs (z, p) of two iteration buffers (16), the
+// off-diagonals (4 W), diag and 1/diag (8) and 16-bit packed columns (2 W).  x, r and q
+// live in registers (each thread owns the same rows for the whole solve).  16 CTAs of
+// R <= 4096 rows hold 65536 rows of width 4.
 size_t cluster_cg_smem_bytes(int R, int W) {
-    return 3 * (size_t)CBS * sizeof(ff) + (size_t)R * (6 * (size_t)W + 20);
+    return 3 * (size_t)CBS * sizeof(ff) + (size_t)R * (6 * (size_t)W + 24);
 }
 
 // largest R whose shared memory fits `optin` bytes per CTA (capped by the 12-bit local
 // index of the packed columns)
 int cluster_cg_max_rows(int W, int optin) {
-    const long long fixed = 3LL * CBS * (long long)sizeof(ff) + 4096;  // tree + static shared memory
-    long long r = ((long long)optin - fixed) / (6LL * W + 20);
+    const long long fixed = 3LL * CBS * (long long)sizeof(ff) + 2048;  // tree + static shared memory
+    long long r = ((long long)optin - fixed) / (6LL * W + 24);
     if (r > 4096) r = 4096;
     return r > 0 ? (int)r : 0;
 }
@@ -42,9 +47,14 @@ int cluster_cg_max_rows(int W, int optin) {
 // rows per thread for R rows per CTA
 int cluster_cg_rpt(int R) { return R <= CBS ? 1 : (R <= 2 * CBS ? 2 : 4); }
 
+__device__ __forceinline__ float2 ld_cluster_f32x2(uint32_t addr) {
+    float2 v;
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
+    return v;
+}
+
 template <int W, int RPT>
 __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
-    constexpr int WA = W > 0 ? W : 1;
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ ff slots[2 * 3 * 16];
     struct Scal {
@@ -59,13 +69,12 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
     const int row0 = (int)me * R;
     const int nloc = max(0, min(R, C - row0));
     ff* sbuf = reinterpret_cast<ff*>(smem);                               // [3][CBS]
-    float* off = reinterpret_cast<float*>(sbuf + 3 * CBS);                // [W][R]
-    float* diag = off + (size_t)W * R;
+    float2* zp0 = reinterpret_cast<float2*>(sbuf + 3 * CBS);              // [R] (z, p) of buffer 0
+    float2* zp1 = zp0 + R;                                                // [R] buffer 1
+    float* off = reinterpret_cast<float*>(zp1 + R);                       // [W][R]
+    float* diag = off + W * R;
     float* invd = diag + R;
-    float* z = invd + R;
-    float* pbuf0 = z + R;
-    float* pbuf1 = pbuf0 + R;
-    uint16_t* colp = reinterpret_cast<uint16_t*>(pbuf1 + R);            // [W][R] (rank << 12) | local
+    uint16_t* colp = reinterpret_cast<uint16_t*>(invd + R);              // [W][R] (rank << 12) | local
     const int t0 = threadIdx.x;
 
     // this CTA's slice of the matrix
@@ -76,15 +85,16 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
         invd[l] = d != 0.0f ? 1.0f / d : 1.0f;
 #pragma unroll
         for (int j = 0; j < W; ++j) {
-            off[(size_t)j * R + l] = a.A.off[(size_t)j * C + g];
+            off[j * R + l] = a.A.off[(size_t)j * C + g];
             const int c = a.m.ell_col[(size_t)j * C + g];
             const int rk = c / R;
-            colp[(size_t)j * R + l] = (uint16_t)((rk << 12) | (c - rk * R));
+            colp[j * R + l] = (uint16_t)((rk << 12) | (c - rk * R));
         }
     }
-    // own rows l = t0 + u CBS, u < RPT: x, r, q in registers
+    // own rows l = t0 + u CBS, u < RPT: x, r, q, p in registers
     float xr[RPT], rr_[RPT], qr[RPT], pr[RPT];
-    // r = b - A x (x read from global) ; z = M r ; p = z ; rr ; rz ; bb
+    // r = b - A x (x read from global) ; z = M r ; first direction p = z (the p half of
+    // buffer 0 is zero and beta 0) ; rr ; rz ; bb
     ff acc[3] = {ff_zero(), ff_zero(), ff_zero()};
 #pragma unroll
     for (int u = 0; u < RPT; ++u) {
@@ -98,13 +108,12 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
             xr[u] = a.x[g];
             float ax = diag[l] * xr[u];
 #pragma unroll
-            for (int j = 0; j < W; ++j) ax += off[(size_t)j * R + l] * a.x[a.m.ell_col[(size_t)j * C + g]];
+            for (int j = 0; j < W; ++j) ax += off[j * R + l] * a.x[a.m.ell_col[(size_t)j * C + g]];
             const float bi = a.A.rhs[g];
             const float ri = bi - ax;
             const float zi = ri * invd[l];
             rr_[u] = ri;
-            z[l] = zi;
-            pbuf0[l] = zi;
+            zp0[l] = make_float2(zi, 0.0f);
             ff_fma(acc[0], ri, ri);
             ff_fma(acc[1], ri, zi);
             ff_fma(acc[2], bi, bi);
@@ -132,34 +141,27 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
     int cur = 0;
     while (sc.go) {
         const float bf = sc.bf;
-        const float* po = cur ? pbuf1 : pbuf0;
-        float* pn = cur ? pbuf0 : pbuf1;
+        // buffer cur holds (z_k, p_{k-1}); p_k and then z_{k+1} go to the other buffer
+        const float2* zpo = cur ? zp1 : zp0;
+        float2* zpn = cur ? zp0 : zp1;
         // p = z + beta p_old (own row and each neighbour) ; q = A p ; p.q
         ff accq[1] = {ff_zero()};
 #pragma unroll
         for (int u = 0; u < RPT; ++u) {
             const int l = t0 + u * CBS;
             if (l < nloc) {
-                const float pi = z[l] + bf * po[l];
+                const float2 own = zpo[l];
+                const float pi = own.x + bf * own.y;
                 float qi = diag[l] * pi;
-                unsigned cp[WA];
-#pragma unroll
-                for (int j = 0; j < W; ++j) cp[j] = colp[(size_t)j * R + l];
 #pragma unroll
                 for (int j = 0; j < W; ++j) {
-                    const unsigned rk = cp[j] >> 12;
-                    const unsigned lo = cp[j] & 0xFFFu;
-                    float zc, pc;
-                    if (rk == me) {
-                        zc = z[lo];
-                        pc = po[lo];
-                    } else {
-                        zc = ld_cluster_f32(map_rank(z + lo, rk));
-                        pc = ld_cluster_f32(map_rank(po + lo, rk));
-                    }
-                    qi += off[(size_t)j * R + l] * (zc + bf * pc);
+                    const unsigned cp = colp[j * R + l];
+                    const unsigned rk = cp >> 12;
+                    const unsigned lo = cp & 0xFFFu;
+                    const float2 v = rk == me ? zpo[lo] : ld_cluster_f32x2(map_rank(zpo + lo, rk));
+                    qi += off[j * R + l] * (v.x + bf * v.y);
                 }
-                pn[l] = pi;
+                zpn[l].y = pi;
                 pr[u] = pi;
                 qr[u] = qi;
                 ff_fma(accq[0], pi, qi);
@@ -190,7 +192,7 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
                 const float ri = rr_[u] - af * qr[u];
                 const float zi = ri * invd[l];
                 rr_[u] = ri;
-                z[l] = zi;
+                zpn[l].x = zi;
                 ff_fma(acc2[0], ri, ri);
                 ff_fma(acc2[1], ri, zi);
             }
