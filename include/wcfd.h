@@ -106,7 +106,8 @@ typedef struct wcfd_krylov_ws {
     double*   partials;   /* 8 * WCFD_MAX_BLOCKS doubles (reduction partials)         */
     double*   results;    /* unused, may be NULL                                      */
     uint32_t* barrier;    /* WCFD_BARRIER_WORDS words: per-block arrival flags, then the
-                             error word; every solve call zeroes them first           */
+                             error word and the aggregator's release word; every
+                             solve call zeroes them first                            */
 } wcfd_krylov_ws;
 
 typedef struct wcfd_solve_stats {

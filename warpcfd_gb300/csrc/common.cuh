@@ -190,17 +190,33 @@ struct GridCtl {
     int* err;
 };
 
+// Bounded wait until *flag >= phase (wrap-safe); false on timeout.
+__device__ __forceinline__ bool wait_flag(const unsigned* flag, unsigned phase) {
+    if ((int)(ld_acquire(flag) - phase) >= 0) return true;
+    const uint64_t t0 = global_ns();
+    unsigned spins = 0;
+    while ((int)(ld_acquire(flag) - phase) < 0) {
+        if ((++spins & 31u) == 0u && global_ns() - t0 > kBarrierTimeoutNs) return false;
+        __nanosleep(64);
+    }
+    return true;
+}
+
 // Barrier + reduction over all blocks of a cooperative launch, for phase number `phase`
 // (1, 2, 3, ... in every block).  v[] holds this block's float-float totals (from
-// block_reduce_ff); on return out[] holds the grid-wide sums (normalised float-float).  Each block
-// publishes its totals and then its flag with one release store (no atomics).  Thread j
-// of every block waits for block j's flag and then fetches block j's totals into shared
-// memory, so the two L2 round trips are paid once, by all threads in parallel; warp 0
-// then merges the totals in a fixed order from shared memory and one thread
-// normalises, so every block gets the same bits on every run.  Totals are double-buffered by
-// phase parity: a block can only overwrite a buffer after every block has passed the
-// phase that read it.  Every wait is bounded: on timeout the block sets *err and returns
-// false.  Requires gridDim.x <= BS.
+// block_reduce_ff); on return out[] holds the grid-wide sums (normalised float-float).
+//
+// Block 0 aggregates: every block publishes its totals and then its arrival flag with one
+// release store; thread j of block 0 waits for block j's flag and fetches block j's totals
+// into shared memory (the L2 round trips paid once, in parallel); warp 0 merges them in
+// block order, thread 0 stores the sums and then releases a single `done` word; thread 0
+// of every other block waits for that word alone and reads the sums.  So every block gets
+// the same bits on every run, and a phase costs about five L2 round trips however many
+// blocks wait: when every thread of every block polled every flag, 233k pollers on a few
+// cache lines made each barrier take ~15 us on a 456-block grid.  Totals and sums are
+// double-buffered by phase parity (the sums in the unused slot WCFD_MAX_BLOCKS - 1): a
+// buffer is rewritten only after every block has passed the phase that read it.  Every
+// wait is bounded: on timeout the block sets *err and returns false.  gridDim.x <= BS.
 template <int NV, int BS>
 __device__ bool grid_sync(const GridCtl& g, const ff* v, ff* out, unsigned phase) {
     static_assert(BS >= 32, "block too small");
@@ -209,6 +225,7 @@ __device__ bool grid_sync(const GridCtl& g, const ff* v, ff* out, unsigned phase
     __shared__ float2 s_part[NV > 0 ? NV : 1][BS];
     if (threadIdx.x == 0) s_fail = 0;
     float2* pb = reinterpret_cast<float2*>(g.partials) + (size_t)(phase & 1u) * 4 * WCFD_MAX_BLOCKS;
+    unsigned* done = g.flags + WCFD_MAX_BLOCKS + 1;
     if constexpr (NV > 0) {
         if (threadIdx.x == 0) {
 #pragma unroll
@@ -218,45 +235,59 @@ __device__ bool grid_sync(const GridCtl& g, const ff* v, ff* out, unsigned phase
     __syncthreads();  // this block's writes of the phase happen before its release
     if (threadIdx.x == 0) st_release(g.flags + blockIdx.x, phase);
     bool ok = true;
-    const int j = threadIdx.x;
-    if (j < (int)gridDim.x) {
-        if ((int)(ld_acquire(g.flags + j) - phase) < 0) {
-            const uint64_t t0 = global_ns();
-            unsigned spins = 0;
-            while ((int)(ld_acquire(g.flags + j) - phase) < 0) {
-                if ((++spins & 31u) == 0u && global_ns() - t0 > kBarrierTimeoutNs) {
-                    ok = false;
-                    break;
-                }
-                __nanosleep(32);
-            }
-        }
-        if constexpr (NV > 0) {
-            if (ok) {
+    if (blockIdx.x == 0) {
+        const int j = threadIdx.x;
+        if (j < (int)gridDim.x) {
+            ok = wait_flag(g.flags + j, phase);
+            if constexpr (NV > 0) {
+                if (ok) {
 #pragma unroll
-                for (int i = 0; i < NV; ++i) s_part[i][j] = __ldcg(pb + i * WCFD_MAX_BLOCKS + j);
+                    for (int i = 0; i < NV; ++i) s_part[i][j] = __ldcg(pb + i * WCFD_MAX_BLOCKS + j);
+                }
+            }
+        }
+        if (!ok) s_fail = 1;
+        __syncthreads();
+        if (!s_fail) {
+            if constexpr (NV > 0) {
+                if (threadIdx.x < 32) {
+                    const int lane = threadIdx.x;
+#pragma unroll
+                    for (int i = 0; i < NV; ++i) {
+                        ff x = ff_zero();
+                        for (int k = lane; k < (int)gridDim.x; k += 32) ff_merge(x, ff{s_part[i][k].x, s_part[i][k].y});
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) ff_shfl_merge(x, o);
+                        if (lane == 0) {
+                            s_res[i] = ff_norm(x);
+                            pb[i * WCFD_MAX_BLOCKS + WCFD_MAX_BLOCKS - 1] = make_float2(s_res[i].hi, s_res[i].lo);
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) st_release(done, phase);  // the sums happen before the release
+        }
+    } else {
+        if (threadIdx.x == 0) {
+            ok = wait_flag(done, phase);
+            if (ok) {
+                if constexpr (NV > 0) {
+#pragma unroll
+                    for (int i = 0; i < NV; ++i) {
+                        const float2 t = __ldcg(pb + i * WCFD_MAX_BLOCKS + WCFD_MAX_BLOCKS - 1);
+                        s_res[i] = ff{t.x, t.y};
+                    }
+                }
+            } else {
+                s_fail = 1;
             }
         }
     }
-    if (!ok) {
-        atomicExch(g.err, WCFD_BARRIER_TIMEOUT);
-        s_fail = 1;
-    }
+    if (s_fail && threadIdx.x == 0) atomicExch(g.err, WCFD_BARRIER_TIMEOUT);
     __syncthreads();
     if (s_fail) return false;
     if constexpr (NV > 0) {
-        if (threadIdx.x < 32) {
-            const int lane = threadIdx.x;
-#pragma unroll
-            for (int i = 0; i < NV; ++i) {
-                ff x = ff_zero();
-                for (int k = lane; k < (int)gridDim.x; k += 32) ff_merge(x, ff{s_part[i][k].x, s_part[i][k].y});
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) ff_shfl_merge(x, o);
-                if (lane == 0) s_res[i] = ff_norm(x);
-            }
-        }
-        __syncthreads();
 #pragma unroll
         for (int i = 0; i < NV; ++i) out[i] = s_res[i];
         __syncthreads();
