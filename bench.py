@@ -457,7 +457,7 @@ def main():
     ap.add_argument("--requests", type=int, default=256, help="serve workload: requests in the mix")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve workload: Poisson arrival rate (1/s)")
     ap.add_argument("--max-outer", type=int, default=4000, help="serve workload: outer-iteration cap per request")
-    ap.add_argument("--drop-in-sample", type=int, default=24, help="serve workload: requests run through the drop-in")
+    ap.add_argument("--drop-in-sample", type=int, default=48, help="serve workload: requests run through the drop-in")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -90,11 +90,15 @@ class FVM:
             return
         _lib.load()
         self.boundary.finalize()
-        geo = build_geometry(self.mesh, correction=False)
         dev = self.device
-        self._geo_host = geo
-        self._geo = {k: (torch.from_numpy(np.ascontiguousarray(v)).to(dev) if isinstance(v, np.ndarray) else v)
-                     for k, v in geo.items()}
+        # the geometry is read-only on the device: models of the same mesh share one copy
+        cache = self.mesh.__dict__.setdefault("_device_geometry", {})
+        key = str(torch.device(dev))
+        if key not in cache:
+            geo = build_geometry(self.mesh, correction=False)
+            cache[key] = (geo, {k: (torch.from_numpy(np.ascontiguousarray(v)).to(dev) if isinstance(v, np.ndarray)
+                                    else v) for k, v in geo.items()})
+        self._geo_host, self._geo = cache[key]
         self.boundary_type = torch.from_numpy(self.boundary.boundary_type.copy()).to(dev)
         self.boundary_value = torch.from_numpy(self.boundary.boundary_values.astype(np.float32)).to(dev)
         self.boundary_ids = self._geo["boundary_face"]

@@ -271,8 +271,8 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
         for (int o = 0; o < 3; ++o) ax[o] = diag[3 * (size_t)i + o] * x[3 * (size_t)i + o];
 #pragma unroll
         for (int j = 0; j < W; ++j) {
-            const float v = off[(size_t)j * C + i];
-            const int c = col[(size_t)j * C + i];
+            const float v = __ldcs(off + (size_t)j * C + i);
+            const int c = __ldcs(col + (size_t)j * C + i);
 #pragma unroll
             for (int o = 0; o < 3; ++o) ax[o] += v * x[3 * (size_t)c + o];
         }
@@ -317,8 +317,8 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
             }
 #pragma unroll
             for (int j = 0; j < W; ++j) {
-                const float v = off[(size_t)j * C + i];
-                const int c = col[(size_t)j * C + i];
+                const float v = __ldcs(off + (size_t)j * C + i);
+                const int c = __ldcs(col + (size_t)j * C + i);
 #pragma unroll
                 for (int o = 0; o < 3; ++o) {
                     const size_t q = 3 * (size_t)c + o;
@@ -361,8 +361,8 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
             }
 #pragma unroll
             for (int j = 0; j < W; ++j) {
-                const float v = off[(size_t)j * C + i];
-                const int c = col[(size_t)j * C + i];
+                const float v = __ldcs(off + (size_t)j * C + i);
+                const int c = __ldcs(col + (size_t)j * C + i);
 #pragma unroll
                 for (int o = 0; o < 3; ++o) {
                     const size_t q = 3 * (size_t)c + o;

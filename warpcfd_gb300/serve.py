@@ -159,12 +159,19 @@ def build_solver(req: Request, mesh, atol=1e-8, maxiter=500, device=None, rtol=(
     return model, solver
 
 
-def case_bytes(model, solver) -> int:
-    """Device bytes held by one admitted case (fields, geometry, systems, workspaces)."""
+def geometry_bytes(model) -> int:
+    """Device bytes of a model's geometry (shared by every model of the same mesh)."""
+    return int(sum(v.numel() * v.element_size() for v in model._geo.values() if isinstance(v, torch.Tensor)))
+
+
+def case_bytes(model, solver, include_geometry=True) -> int:
+    """Device bytes held by one admitted case (fields, systems, workspaces and, unless
+    include_geometry is False, the mesh geometry it shares with other cases of its mesh)."""
     ts = [model.cell_values, model.cell_gradients, model.face_values, model.face_gradients, model.mass_fluxes,
           model.boundary_type, model.boundary_value, solver.rUA, solver.rUA_faces, solver.div_u,
           solver.vel_correction, solver.stats]
-    ts += [v for v in model._geo.values() if isinstance(v, torch.Tensor)]
+    if include_geometry:
+        ts += [v for v in model._geo.values() if isinstance(v, torch.Tensor)]
     for e in (solver.vel_equation, solver.p_corr_equation):
         ts += [e.diag, e.off, e.rhs, e.x, e.ws_vec, e.ws_partials, e.ws_results, e.ws_barrier, e.stats]
     return int(sum(t.numel() * t.element_size() for t in ts))
@@ -194,6 +201,7 @@ class ServeReport:
     max_active: int = 0
     peak_bytes: int = 0
     bucket_busy_s: list = field(default_factory=list)
+    admit_s: float = 0.0
 
     def summary(self):
         lat = np.array([r.latency for r in self.results]) if self.results else np.zeros(1)
@@ -213,13 +221,14 @@ class ServeReport:
             "max_active": self.max_active,
             "peak_case_bytes": self.peak_bytes,
             "bucket_gpu_busy_s": [round(x, 3) for x in self.bucket_busy_s],
+            "host_admission_s": round(self.admit_s, 3),
         }
 
 
 class Server:
     """Continuous batching over size buckets (bucket = cell count up to its bound)."""
 
-    def __init__(self, hbm_budget=16 << 30, max_active=96, tol=1e-6, check_every=10, max_outer=4000,
+    def __init__(self, hbm_budget=16 << 30, max_active=256, tol=1e-6, check_every=10, max_outer=4000,
                  buckets=(4096, 8192, 16384, 32768, 65536), atol=SERVE_ATOL, rtol=SERVE_RTOL, device=None,
                  clock=time.perf_counter, keep_fields=False):
         self.budget = int(hbm_budget)
@@ -233,6 +242,8 @@ class Server:
         self.device = device or torch.device("cuda", torch.cuda.current_device())
         self.clock = clock
         self.meshes = MeshCache()
+        self._geometry_charged = set()
+        self._geometry_bytes = 0
         self.keep_fields = keep_fields
         self.streams = [torch.cuda.Stream(device=self.device) for _ in self.bounds]
         # one cluster size per bucket, from its bound, so a case's arithmetic never depends
@@ -259,9 +270,15 @@ class Server:
         return len(self.bounds) - 1
 
     def _admit(self, req, t0):
+        """Build the case (the mesh and its device geometry come from caches) and charge its
+        device bytes; a mesh's geometry is charged once, when it first reaches the device."""
         mesh = self.meshes.get(req.kind, req.cells)
         model, solver = build_solver(req, mesh, atol=self.atol, device=self.device, rtol=self.rtol)
-        return _Slot(req, model, solver, case_bytes(model, solver), self.clock() - t0)
+        nb = case_bytes(model, solver, include_geometry=False)
+        if id(mesh) not in self._geometry_charged:
+            self._geometry_charged.add(id(mesh))
+            self._geometry_bytes += geometry_bytes(model)
+        return _Slot(req, model, solver, nb, self.clock() - t0)
 
     def run(self, requests) -> ServeReport:
         """Serve ``requests`` (arrival times relative to the start of the call).
@@ -292,11 +309,14 @@ class Server:
             now = self.clock() - t0
             while qi < len(pending) and pending[qi].arrival <= now:
                 n_live = sum(len(a) for a in active) + sum(len(a) for a in incoming)
-                if n_live >= self.max_active or used + estimate_bytes(pending[qi].cells) > self.budget:
+                if n_live >= self.max_active or (used + self._geometry_bytes + estimate_bytes(pending[qi].cells)
+                                                 > self.budget):
                     break
+                ta = self.clock()
                 slot = self._admit(pending[qi], t0)
+                report.admit_s += self.clock() - ta
                 used += slot.bytes
-                report.peak_bytes = max(report.peak_bytes, used)
+                report.peak_bytes = max(report.peak_bytes, used + self._geometry_bytes)
                 incoming[self._bucket(slot.model.num_cells)].append(slot)
                 qi += 1
             report.max_active = max(report.max_active, sum(len(a) for a in active) + sum(len(a) for a in incoming))
