@@ -57,6 +57,7 @@ template <int W, int RPT>
 __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ ff slots[2 * 3 * 16];
+    __shared__ unsigned char chunk_local[4096 / 32];  // 32-row chunk with no off-CTA neighbour
     struct Scal {
         ff rr, rz, pq, thr2;
         float af, bf;
@@ -83,13 +84,18 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
         const float d = a.A.diag[g];
         diag[l] = d;
         invd[l] = d != 0.0f ? 1.0f / d : 1.0f;
+        bool local = true;
 #pragma unroll
         for (int j = 0; j < W; ++j) {
             off[j * R + l] = a.A.off[(size_t)j * C + g];
             const int c = a.m.ell_col[(size_t)j * C + g];
             const int rk = c / R;
             colp[j * R + l] = (uint16_t)((rk << 12) | (c - rk * R));
+            local = local && rk == (int)me;
         }
+        // a warp's lanes hold the 32 consecutive rows of one chunk, here and in the passes
+        local = __all_sync(__activemask(), local);
+        if ((t0 & 31) == 0) chunk_local[l >> 5] = local ? 1 : 0;
     }
     // own rows l = t0 + u CBS, u < RPT: x, r, q, p in registers
     float xr[RPT], rr_[RPT], qr[RPT], pr[RPT];
@@ -153,13 +159,21 @@ __device__ __forceinline__ void cg_cluster_body(const KrylovArgs& a, int R) {
                 const float2 own = zpo[l];
                 const float pi = own.x + bf * own.y;
                 float qi = diag[l] * pi;
+                if (chunk_local[l >> 5]) {  // warp-uniform: every neighbour in this CTA
 #pragma unroll
-                for (int j = 0; j < W; ++j) {
-                    const unsigned cp = colp[j * R + l];
-                    const unsigned rk = cp >> 12;
-                    const unsigned lo = cp & 0xFFFu;
-                    const float2 v = rk == me ? zpo[lo] : ld_cluster_f32x2(map_rank(zpo + lo, rk));
-                    qi += off[j * R + l] * (v.x + bf * v.y);
+                    for (int j = 0; j < W; ++j) {
+                        const float2 v = zpo[colp[j * R + l] & 0xFFFu];
+                        qi += off[j * R + l] * (v.x + bf * v.y);
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < W; ++j) {
+                        const unsigned cp = colp[j * R + l];
+                        const unsigned rk = cp >> 12;
+                        const unsigned lo = cp & 0xFFFu;
+                        const float2 v = rk == me ? zpo[lo] : ld_cluster_f32x2(map_rank(zpo + lo, rk));
+                        qi += off[j * R + l] * (v.x + bf * v.y);
+                    }
                 }
                 zpn[l].y = pi;
                 pr[u] = pi;

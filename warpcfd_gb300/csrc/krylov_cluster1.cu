@@ -37,6 +37,7 @@ template <int W, int RPT>
 __device__ __forceinline__ void cg1_cluster_body(const KrylovArgs& a, int R) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ ff slots[2 * 3 * 16];
+    __shared__ unsigned char chunk_local[4096 / 32];  // 32-row chunk with no off-CTA neighbour
     struct Scal {
         ff rr, gamma, thr2;
         float af, bf, alpha_prev;
@@ -59,13 +60,17 @@ __device__ __forceinline__ void cg1_cluster_body(const KrylovArgs& a, int R) {
     for (int l = t0; l < nloc; l += CBS) {
         const int g = row0 + l;
         diag[l] = a.A.diag[g];
+        bool local = true;
 #pragma unroll
         for (int j = 0; j < W; ++j) {
             off[j * R + l] = a.A.off[(size_t)j * C + g];
             const int c = a.m.ell_col[(size_t)j * C + g];
             const int rk = c / R;
             colp[j * R + l] = (uint16_t)((rk << 12) | (c - rk * R));
+            local = local && rk == (int)me;
         }
+        local = __all_sync(__activemask(), local);
+        if ((t0 & 31) == 0) chunk_local[l >> 5] = local ? 1 : 0;
     }
     // r0 = b - A x0 ; buffer 0 = (r0, 0, 0, 1/d) ; r0.r0 ; b.b
     float xr[RPT], pr[RPT], sr[RPT], rr_[RPT], ur[RPT], wr[RPT];
@@ -126,14 +131,22 @@ __device__ __forceinline__ void cg1_cluster_body(const KrylovArgs& a, int R) {
                 const float ui = ri * own.w;
                 // w = A u, the neighbours' u formed from their previous (r, w, s)
                 float wi = diag[l] * ui;
+                if (chunk_local[l >> 5]) {  // warp-uniform: every neighbour in this CTA
 #pragma unroll
-                for (int j = 0; j < W; ++j) {
-                    const unsigned cp = colp[j * R + l];
-                    const unsigned rk = cp >> 12;
-                    const unsigned lo = cp & 0xFFFu;
-                    const float4 v = rk == me ? rbo[lo] : ld_cluster_f32x4(map_rank(rbo + lo, rk));
-                    const float uc = (v.x - af * (v.y + bf * v.z)) * v.w;
-                    wi += off[j * R + l] * uc;
+                    for (int j = 0; j < W; ++j) {
+                        const float4 v = rbo[colp[j * R + l] & 0xFFFu];
+                        wi += off[j * R + l] * ((v.x - af * (v.y + bf * v.z)) * v.w);
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < W; ++j) {
+                        const unsigned cp = colp[j * R + l];
+                        const unsigned rk = cp >> 12;
+                        const unsigned lo = cp & 0xFFFu;
+                        const float4 v = rk == me ? rbo[lo] : ld_cluster_f32x4(map_rank(rbo + lo, rk));
+                        const float uc = (v.x - af * (v.y + bf * v.z)) * v.w;
+                        wi += off[j * R + l] * uc;
+                    }
                 }
                 rbn[l] = make_float4(ri, wi, si, own.w);
                 sr[u] = si;
