@@ -270,6 +270,19 @@ int wcfd_cg_noalloc(const wcfd_mesh* m, wcfd_system A, float* x, double atol, in
  * fused kernels on `stream`; capturable in a CUDA graph. */
 int wcfd_simple_iteration(const wcfd_case* c, void* stream);
 
+/* ------------------------------------------------------------------ convergence monitor
+ * The residual norms of FVM.check_convergence (model.py:278-316, criteria of
+ * Convergence.py:53-61) in one fused device pass: out (9 DEVICE doubles) receives
+ * ||A x - b||_2 for the three momentum components (A: the momentum system, ncomp 3;
+ * x: 3C interleaved velocity), ||b||_2 of each component, ||div||_1, ||rUA grad p||_inf
+ * (cell_gradients C x 4 x 3, rua C) and ||p||_inf.  div, cell_gradients/rua and p may be
+ * NULL (their norms are then 0).  scratch: wcfd_convergence_scratch_floats() floats of
+ * device memory.  Two launches; the sums are float-float and reproducible. */
+int64_t wcfd_convergence_scratch_floats(void);
+int wcfd_convergence_norms(const wcfd_mesh* m, wcfd_system A, const float* x, const float* div,
+                           const float* cell_gradients, const float* rua, const float* p, float* scratch,
+                           double* out, void* stream);
+
 /* ------------------------------------------------------------------ batched form
  * Many cases in one launch per kernel: `cases` is a DEVICE array of wcfd_case (a case
  * table; each entry points at that case's own arrays).  Field and assembly kernels run

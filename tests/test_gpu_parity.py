@@ -377,3 +377,31 @@ def test_relative_krylov_stop(path):
             assert torch.equal(xa, xb)
     finally:
         lib.wcfd_set_krylov_path(0)
+
+
+def test_device_convergence_monitor_matches_reference_norms():
+    """wcfd_convergence_norms (one fused pass) gives the norms of model.py:278-316 computed
+    the reference's way (torch fp64 over the same arrays)."""
+    m = cavity_mesh(24, jitter=0.1, seed=4)
+    model, solver, _ = make_pair(m, cavity_bc)
+    for _ in range(3):
+        solver.step()
+    torch.cuda.synchronize()
+    ve = solver.vel_equation
+    norms = model.convergence_norms(ve.system_struct(), solver.HbyA, solver.div_u, solver.rUA,
+                                    solver.p_corr_equation.x)
+    Ax = ve.apply(solver.HbyA).reshape(-1, 3).double()
+    b = ve.rhs.reshape(-1, 3).double()
+    ref = [float(torch.linalg.vector_norm(Ax[:, o] - b[:, o])) for o in range(3)]
+    ref += [float(torch.linalg.vector_norm(b[:, o])) for o in range(3)]
+    div = model.divFlux(solver.div_u).double()
+    ref.append(float(div.abs().sum()))
+    vc = model.cell_gradients[:, 3, :].double() * solver.rUA.double()[:, None]
+    ref.append(float(vc.abs().max()))
+    ref.append(float(solver.p_corr_equation.x.double().abs().max()))
+    for k, (got, want) in enumerate(zip(norms, ref)):
+        # the residual is a difference of fp32 SpMV results: both sides round A x in fp32
+        tol = 1e-4 if k < 3 else 1e-6
+        assert abs(got - want) <= tol * max(abs(want), 1e-30) + 1e-12, (k, got, want)
+    conv, _ = model.check_convergence_norms(norms)
+    assert set(conv) >= {"momentum_x", "continuity", "velocity_correction", "pressure_correction"}

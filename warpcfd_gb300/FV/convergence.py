@@ -48,6 +48,12 @@ class Criteria:
         self.is_converged = res < self.eps
         return res, self.is_converged
 
+    def check_norms(self, res_norm, rhs_norm=0.0):
+        """check() from norms computed elsewhere (the device convergence monitor)."""
+        res = res_norm if self.tol == "abs" else res_norm / max(rhs_norm, self.non_zero)
+        self.is_converged = res < self.eps
+        return res, self.is_converged
+
 
 class Convergence:
     """Criteria of Convergence.py:53-61: continuity L1 abs 1e-4; momentum L2 relative
@@ -67,6 +73,9 @@ class Convergence:
 
     def check(self, criteria: str, arr, rhs=0.0, ord=None):
         return getattr(self, criteria).check(arr, rhs, ord)
+
+    def check_norms(self, criteria: str, res_norm, rhs_norm=0.0):
+        return getattr(self, criteria).check_norms(res_norm, rhs_norm)
 
     def has_converged(self):
         return all(c.is_converged for c in self.criterias)

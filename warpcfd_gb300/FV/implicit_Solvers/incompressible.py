@@ -216,9 +216,10 @@ class IncompressibleSolver:
     def report(self, steps):
         ve = self.vel_equation
         st = self.solve_stats()
-        vc = self.model.cell_gradients[:, 3, :].reshape(-1) * self.rUA.repeat_interleave(3)
-        conv, converged = self.model.check_convergence(ve.apply, self.HbyA, ve.rhs, self.div_u, vc,
-                                                       self.p_corr_equation.x)
+        # the norms of model.py:278-316 from the device convergence monitor (one fused pass)
+        norms = self.model.convergence_norms(ve.system_struct(), self.HbyA, self.div_u, self.rUA,
+                                             self.p_corr_equation.x)
+        conv, converged = self.model.check_convergence_norms(norms)
         if self.verbose:
             print(f"step iter: {steps}")
             print(f"Outer loop Linear Solve {st[0]} Inner loop solve {st[1]}:")

@@ -249,6 +249,36 @@ class FVM:
             raise ValueError("Only cell or face struct members can be returned")
         return np.asarray(src[member])
 
+    def convergence_norms(self, vel_system, velocity, div_u=None, rua=None, p=None):
+        """The nine residual norms of check_convergence from one fused device pass
+        (wcfd_convergence_norms): ||A u - b||_2 and ||b||_2 per momentum component,
+        ||div||_1, ||rUA grad p||_inf (from cell_gradients and rua), ||p||_inf."""
+        if getattr(self, "_norm_scratch", None) is None:
+            n = int(_lib.load().wcfd_convergence_scratch_floats())
+            self._norm_scratch = torch.empty(n, dtype=torch.float32, device=self.device)
+            self._norm_out = torch.empty(9, dtype=torch.float64, device=self.device)
+        _lib.call("wcfd_convergence_norms", ct.byref(self.mesh_struct()), vel_system, _ptr(velocity),
+                  _ptr(div_u) if div_u is not None else None,
+                  _ptr(self.cell_gradients) if rua is not None else None,
+                  _ptr(rua) if rua is not None else None, _ptr(p) if p is not None else None,
+                  _ptr(self._norm_scratch), _ptr(self._norm_out), _stream())
+        return self._norm_out.cpu().numpy()
+
+    def check_convergence_norms(self, norms, log=True):
+        """check_convergence from convergence_norms()."""
+        conv = {}
+        for o, name in enumerate(("momentum_x", "momentum_y", "momentum_z")):
+            conv[name] = self.Convergence.check_norms(name, float(norms[o]), float(norms[3 + o]))
+        conv["continuity"] = self.Convergence.check_norms("continuity", float(norms[6]))
+        conv["local_continuity"] = self.Convergence.check_norms("local_continuity", float(norms[6]))
+        conv["velocity_correction"] = self.Convergence.check_norms("velocity_correction", float(norms[7]))
+        conv["pressure_correction"] = self.Convergence.check_norms("pressure_correction", float(norms[8]))
+        if log:
+            self.Convergence.log(conv)
+        if np.isnan(conv["momentum_x"][0]):
+            raise ValueError("NaN in the momentum residual")
+        return conv, self.Convergence.has_converged()
+
     def check_convergence(self, vel_matrix, velocity, b, div_u=None, velocity_correction=None, p_correction=None,
                           log=True):
         """Residual norms of model.py:278-316 (fp64 on the device).  ``vel_matrix`` is a

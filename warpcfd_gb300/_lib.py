@@ -115,6 +115,8 @@ _SIGS = {
     "wcfd_cg_noalloc": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, ct.c_double, ct.c_int32, vp, vp]),
     "wcfd_batch_cluster_size": (ct.c_int, [ct.POINTER(BatchDims_t)]),
     "wcfd_batch_max_rows": (ct.c_int, [ct.c_int32]),
+    "wcfd_convergence_scratch_floats": (ct.c_int64, []),
+    "wcfd_convergence_norms": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, vp, vp, vp, vp, vp, vp, vp]),
     "wcfd_batch_simple_iteration": (ct.c_int, [vp, ct.c_int32, ct.POINTER(BatchDims_t), vp]),
     "wcfd_batch_last_error": (ct.c_char_p, []),
 }
