@@ -43,6 +43,17 @@ WORKLOADS = {
 }
 METRIC = "cell-iterations/s"
 
+# DRAM bytes (read + written) of the dominant kernel measured with ncu
+# (`dram__bytes_read.sum + dram__bytes_write.sum`, one capture per workload):
+#   channel   cg_cluster_kernel: 1.47 MB per launch whatever the iteration count (the
+#             system is read once into shared memory)
+#   cavity3d  cg_kernel: 21.08 GB for a 174-iteration launch = 121.2 MB per iteration
+#             (the vectors stay in L2; the matrix streams)
+MEASURED_TRAFFIC = {
+    "channel": {"per_launch": 1.473e6, "per_iteration": 0.0},
+    "cavity3d": {"per_launch": 0.0, "per_iteration": 21.08e9 / 174},
+}
+
 
 def build_mesh(workload):
     from warpcfd_gb300.preprocess import (Mesh, create_2D_grid, create_3D_grid, create_cylinder_channel_grid,
@@ -409,10 +420,17 @@ def run_ours(args):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     if cg_ms.sum() >= bicg_ms.sum():
-        kname, kbytes, kms, nl = "cg_kernel", cg_bytes, cg_ms.sum(), K_
+        from warpcfd_gb300 import _lib
+        rows = int(_lib.load().wcfd_batch_max_rows(W))  # rows per CTA of the cluster-resident CG
+        kname = "cg_cluster_kernel" if C <= 16 * rows else "cg_kernel"
+        kbytes, kms, nl = cg_bytes, cg_ms.sum(), K_
     else:
         kname, kbytes, kms, nl = "bicgstab_kernel", bi_bytes, bicg_ms.sum(), K_
     achieved = kbytes / (kms * 1e-3) / 1e9
+    traffic = None
+    mt = MEASURED_TRAFFIC.get(args.workload)
+    if mt is not None and kname.startswith("cg"):
+        traffic = mt["per_launch"] + mt["per_iteration"] * float(k_p.mean())
     step_bytes = [perfmodel.simple_step_bytes(C, K, Ki, B, F, W, int(a), int(b))["total"] for a, b in zip(k_u, k_p)]
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K_, "warmup": args.warmup,
@@ -428,7 +446,9 @@ def run_ours(args):
         "gpu_launches": (6 + 7 * solver.NUM_INNER_LOOPS) * K_,
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks
-                     else "fallback", "traffic": None,
+                     else "fallback", "traffic": traffic,
+                     "traffic_note": "ncu DRAM bytes per launch of this kernel on this workload (one capture, "
+                                     "scaled by the mean iteration count)" if traffic is not None else None,
                      "bytes_per_launch": kbytes / nl, "ms_per_launch": kms / nl,
                      "step_bytes_per_s_GBs": float(np.sum(step_bytes) / (total_ms * 1e-3) / 1e9)},
         "kernel_ms": {"bicgstab": float(bicg_ms.mean()), "cg": float(cg_ms.mean()), "step": float(step_ms.mean())},
