@@ -298,7 +298,9 @@ typedef struct wcfd_batch_dims {
     int32_t n_inner;         /* pressure correctors                    */
     int32_t n_ortho;         /* non-orthogonal correctors              */
     int32_t cluster_size;    /* CTAs per case for the solves; 0 = pick */
-    int32_t pad_;
+    int32_t field_block;     /* threads per block of the field/assembly kernels: 0 = 256,
+                                else 64..512 in steps of 32 (the result does not depend
+                                on it: those kernels compute each face or cell alone)  */
 } wcfd_batch_dims;
 
 /* Cluster size wcfd_batch_simple_iteration would pick for these dims (0 = no cluster
@@ -309,6 +311,10 @@ int wcfd_batch_cluster_size(const wcfd_batch_dims* dims);
  * off-diagonal width (a cluster of cs CTAs takes cases of up to cs times as many cells;
  * the fewest CTAs per case give the most cases in flight). */
 int wcfd_batch_max_rows(int32_t ell_width);
+/* Set up, on the current device, everything a batched step with these dims needs before
+ * its first launch (the cluster kernels' launch attributes), so that the step can be
+ * captured into a CUDA graph without a first-use host call inside the capture. */
+int wcfd_batch_prepare(const wcfd_batch_dims* dims);
 
 /* One SIMPLE outer iteration (or PISO step) of every case in the table
  * (incompressible.py:95-156 for each case). */

@@ -73,3 +73,37 @@ def test_batch_rejects_mixed_widths():
     m3, s3, _ = make_pair(cavity3d_mesh(4), cavity3d_bc)
     with pytest.raises(ValueError):
         CaseBatch([s2, s3])
+
+
+def test_graph_replay_field_block_and_autotune_keep_results():
+    """CaseBatch.steps (a captured CUDA graph of n batched steps), any field block size and
+    the autotuner's timed trial steps leave every case's result bit for bit as eager
+    steps at the default block size give it."""
+    from warpcfd_gb300.autotune import tune_field_block
+    from warpcfd_gb300.batch import CaseBatch
+
+    ref = _cases()
+    b_ref = CaseBatch([s for _, s in ref])
+    for _ in range(6):
+        b_ref.step()
+    want = [fields(m) for m, _ in ref]
+
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        graphed = _cases()
+        b = CaseBatch([s for _, s in graphed], field_block=128)
+        b.steps(3)
+        b.steps(3)  # replays the graph captured by the first call
+    torch.cuda.current_stream().wait_stream(side)
+    for i, (m, _) in enumerate(graphed):
+        assert np.array_equal(fields(m), want[i]), i
+
+    tuned = _cases()
+    b2 = CaseBatch([s for _, s in tuned])
+    fb = tune_field_block(b2, key=("test", 1))
+    assert fb in (128, 256, 512) and b2.field_block == fb
+    for _ in range(6):
+        b2.step()
+    for i, (m, _) in enumerate(tuned):
+        assert np.array_equal(fields(m), want[i]), i

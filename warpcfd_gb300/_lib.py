@@ -85,7 +85,7 @@ class Case_t(ct.Structure):
 class BatchDims_t(ct.Structure):
     _fields_ = [("max_cells", ct.c_int32), ("max_faces", ct.c_int32), ("faces_per_cell", ct.c_int32),
                 ("ell_width", ct.c_int32), ("n_inner", ct.c_int32), ("n_ortho", ct.c_int32),
-                ("cluster_size", ct.c_int32), ("pad_", ct.c_int32)]
+                ("cluster_size", ct.c_int32), ("field_block", ct.c_int32)]
 
 
 # name -> (restype, argtypes)
@@ -115,6 +115,7 @@ _SIGS = {
     "wcfd_cg_noalloc": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, ct.c_double, ct.c_int32, vp, vp]),
     "wcfd_batch_cluster_size": (ct.c_int, [ct.POINTER(BatchDims_t)]),
     "wcfd_batch_max_rows": (ct.c_int, [ct.c_int32]),
+    "wcfd_batch_prepare": (ct.c_int, [ct.POINTER(BatchDims_t)]),
     "wcfd_convergence_scratch_floats": (ct.c_int64, []),
     "wcfd_convergence_norms": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, vp, vp, vp, vp, vp, vp, vp]),
     "wcfd_batch_simple_iteration": (ct.c_int, [vp, ct.c_int32, ct.POINTER(BatchDims_t), vp]),

@@ -18,7 +18,11 @@ from . import _lib
 
 
 class CaseBatch:
-    def __init__(self, solvers, cluster_size: int = 0, device=None):
+    """``cluster_size``: CTAs per case for the Krylov solves (0 = the library's pick);
+    ``field_block``: threads per block of the field and assembly kernels (0 = 256; see
+    warpcfd_gb300.autotune)."""
+
+    def __init__(self, solvers, cluster_size: int = 0, device=None, field_block: int = 0):
         if not solvers:
             raise ValueError("a batch needs at least one case")
         self.solvers = list(solvers)
@@ -38,12 +42,18 @@ class CaseBatch:
         self.dims = _lib.BatchDims_t(
             max(s.model.num_cells for s in self.solvers), max(s.model.num_faces for s in self.solvers),
             self.faces_per_cell, self.ell_width, self.solvers[0].NUM_INNER_LOOPS,
-            self.solvers[0].NUM_ORTHOGONAL_CORRECTORS, int(cluster_size), 0)
+            self.solvers[0].NUM_ORTHOGONAL_CORRECTORS, int(cluster_size), int(field_block))
+        self._graph = None
+        self._graph_steps = 0
         self.table = torch.empty(n * ct.sizeof(_lib.Case_t), dtype=torch.uint8, device=self.device)
         self.refresh()
 
     def __len__(self):
         return len(self.solvers)
+
+    @property
+    def field_block(self) -> int:
+        return self.dims.field_block or 256
 
     @property
     def cluster_size(self) -> int:
@@ -70,6 +80,23 @@ class CaseBatch:
                                              ct.c_void_p(torch.cuda.current_stream().cuda_stream))
         if rc != 0:
             raise _lib.WcfdError(rc, lib.wcfd_batch_last_error().decode(errors="replace"))
+
+    def steps(self, n: int):
+        """n outer iterations of every case as one CUDA graph replay on the current stream
+        (the graph of n batched steps is captured on first use, without running them, and
+        kept while the batch lives: the launch sequence depends only on the dims).  The
+        current stream must not be the legacy default stream."""
+        if self._graph is None or self._graph_steps != n:
+            _lib.check(_lib.load().wcfd_batch_prepare(ct.byref(self.dims)))
+            g = torch.cuda.CUDAGraph()
+            g.capture_begin(capture_error_mode="thread_local")
+            try:
+                for _ in range(n):
+                    self.step()
+            finally:
+                g.capture_end()
+            self._graph, self._graph_steps = g, n
+        self._graph.replay()
 
     def solve_stats(self):
         """Per case: [(momentum stats), (pressure stats)] as numpy records."""

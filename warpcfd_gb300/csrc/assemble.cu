@@ -191,16 +191,16 @@ void launch_spmv(const wcfd_mesh& m, wcfd_system A, const float* x, float* y, cu
 // Batched assembly over a device case table (blockIdx.y = case).
 namespace wcfd {
 
-__global__ void __launch_bounds__(kBlock) momentum_assemble_batched(const wcfd_case* __restrict__ cases) {
+__global__ void __launch_bounds__(kMaxFieldBlock) momentum_assemble_batched(const wcfd_case* __restrict__ cases) {
     const wcfd_case& c = cases[blockIdx.y];
-    const int i = blockIdx.x * kBlock + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.mesh.n_cells) return;
     momentum_assemble_body(c.mesh, c.bc, c.state, c.mom, c.rua, c.prm, i);
 }
 
-__global__ void __launch_bounds__(kBlock) pressure_assemble_batched(const wcfd_case* __restrict__ cases) {
+__global__ void __launch_bounds__(kMaxFieldBlock) pressure_assemble_batched(const wcfd_case* __restrict__ cases) {
     const wcfd_case& c = cases[blockIdx.y];
-    const int i = blockIdx.x * kBlock + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.mesh.n_cells) return;
     pressure_assemble_body(c.mesh, c.bc, c.state, c.pres, c.rua_faces, c.div, c.prm, i);
 }

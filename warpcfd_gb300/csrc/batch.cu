@@ -31,7 +31,9 @@ int pick_cluster(const wcfd_batch_dims& d) {
     return 0;
 }
 
-int launch_cluster(const void* fn, int n_cases, int cs, size_t smem, cudaStream_t st, void** args) {
+// the launch attributes a cluster kernel needs (dynamic shared memory, non-portable
+// cluster size), set once per (kernel, device, size); 0 on success
+int prepare_cluster(const void* fn, size_t smem) {
     static std::mutex mu;
     static size_t set_bytes[128] = {0};
     static const void* set_fn[128] = {nullptr};
@@ -62,6 +64,12 @@ int launch_cluster(const void* fn, int n_cases, int cs, size_t smem, cudaStream_
             set_bytes[slot] = smem;
         }
     }
+    return WCFD_OK;
+}
+
+int launch_cluster(const void* fn, int n_cases, int cs, size_t smem, cudaStream_t st, void** args) {
+    const int rc = prepare_cluster(fn, smem);
+    if (rc) return rc;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(n_cases * cs);
     cfg.blockDim = dim3(kClusterBlock);
@@ -96,6 +104,19 @@ int launch_cluster(const void* fn, int n_cases, int cs, size_t smem, cudaStream_
 
 extern "C" const char* wcfd_batch_last_error(void) { return g_batch_error; }
 
+extern "C" int wcfd_batch_prepare(const wcfd_batch_dims* dims) {
+    if (!dims || dims->max_cells <= 0 || dims->ell_width < 0 || dims->ell_width > kMaxSlots) return WCFD_ERR_ARGUMENT;
+    const int cs = dims->cluster_size > 0 ? dims->cluster_size : pick_cluster(*dims);
+    if (cs < 1 || cs > 16) return WCFD_ERR_TOO_LARGE;
+    const int R = (dims->max_cells + cs - 1) / cs;
+    const void* cg_fn = cg_cluster_batched_for(dims->ell_width, R);
+    const void* bi_fn = bicgstab_cluster_batched_for(dims->ell_width);
+    if (!cg_fn || !bi_fn) return WCFD_ERR_ARGUMENT;
+    int rc = prepare_cluster(bi_fn, 0);
+    if (!rc) rc = prepare_cluster(cg_fn, cluster_cg_smem_bytes(R, dims->ell_width));
+    return rc;
+}
+
 extern "C" int wcfd_batch_max_rows(int32_t ell_width) {
     if (ell_width < 0 || ell_width > kMaxSlots) return 0;
     return batch_budget_rows(ell_width);
@@ -118,6 +139,11 @@ extern "C" int wcfd_batch_simple_iteration(const wcfd_case* cases, int32_t n_cas
         std::snprintf(g_batch_error, sizeof(g_batch_error), "bad batch dims");
         return WCFD_ERR_ARGUMENT;
     }
+    const int fb = d.field_block > 0 ? d.field_block : kBlock;
+    if (fb < 64 || fb > kMaxFieldBlock || fb % 32 != 0) {
+        std::snprintf(g_batch_error, sizeof(g_batch_error), "field_block must be 64..%d in steps of 32", kMaxFieldBlock);
+        return WCFD_ERR_ARGUMENT;
+    }
     const int cs = d.cluster_size > 0 ? d.cluster_size : pick_cluster(d);
     if (cs < 1 || cs > 16) {
         std::snprintf(g_batch_error, sizeof(g_batch_error), "no cluster size fits max_cells %d", d.max_cells);
@@ -132,41 +158,41 @@ extern "C" int wcfd_batch_simple_iteration(const wcfd_case* cases, int32_t n_cas
     const void* bi_fn = bicgstab_cluster_batched_for(d.ell_width);
     if (!cg_fn || !bi_fn) return WCFD_ERR_ARGUMENT;
     cudaStream_t st = S(stream);
-    const dim3 gf(grid_for(d.max_faces), n_cases), gc(grid_for(d.max_cells), n_cases);
+    const dim3 gf((d.max_faces + fb - 1) / fb, n_cases), gc((d.max_cells + fb - 1) / fb, n_cases);
     // incompressible.py:96-99
-    face_pass_batched<<<gf, kBlock, 0, st>>>(cases, WCFD_ALL, 1u | 2u);
+    face_pass_batched<<<gf, fb, 0, st>>>(cases, WCFD_ALL, 1u | 2u);
     BCHECK("face_pass_batched");
-    gradient_batched<<<gc, kBlock, 0, st>>>(cases, WCFD_ALL, 0);
+    gradient_batched<<<gc, fb, 0, st>>>(cases, WCFD_ALL, 0);
     BCHECK("gradient_batched");
     // :102-116
-    momentum_assemble_batched<<<gc, kBlock, 0, st>>>(cases);
+    momentum_assemble_batched<<<gc, fb, 0, st>>>(cases);
     BCHECK("momentum_assemble_batched");
     int csv = cs;
     void* bargs[] = {(void*)&cases, &csv};
     int rc = launch_cluster(bi_fn, n_cases, cs, 0, st, bargs);
     if (rc) return rc;
     // :118-123
-    hbya_batched<<<gc, kBlock, 0, st>>>(cases);
+    hbya_batched<<<gc, fb, 0, st>>>(cases);
     BCHECK("hbya_batched");
-    rua_faces_batched<<<gf, kBlock, 0, st>>>(cases);
+    rua_faces_batched<<<gf, fb, 0, st>>>(cases);
     BCHECK("rua_faces_batched");
     const size_t smem = cluster_cg_smem_bytes(R, d.ell_width);
     for (int inner = 0; inner < d.n_inner; ++inner) {
         for (int ortho = 0; ortho < d.n_ortho; ++ortho) {
-            face_pass_batched<<<gf, kBlock, 0, st>>>(cases, WCFD_ALL, 2u);
+            face_pass_batched<<<gf, fb, 0, st>>>(cases, WCFD_ALL, 2u);
             BCHECK("face_pass_batched");
-            gradient_batched<<<gc, kBlock, 0, st>>>(cases, WCFD_ALL, 1);
+            gradient_batched<<<gc, fb, 0, st>>>(cases, WCFD_ALL, 1);
             BCHECK("gradient_batched");
-            pressure_assemble_batched<<<gc, kBlock, 0, st>>>(cases);
+            pressure_assemble_batched<<<gc, fb, 0, st>>>(cases);
             BCHECK("pressure_assemble_batched");
             void* cargs[] = {(void*)&cases, &csv};
             rc = launch_cluster(cg_fn, n_cases, cs, smem, st, cargs);
             if (rc) return rc;
-            p_update_batched<<<gc, kBlock, 0, st>>>(cases);
+            p_update_batched<<<gc, fb, 0, st>>>(cases);
             BCHECK("p_update_batched");
-            face_pass_batched<<<gf, kBlock, 0, st>>>(cases, WCFD_P, 0u);
+            face_pass_batched<<<gf, fb, 0, st>>>(cases, WCFD_P, 0u);
             BCHECK("face_pass_batched");
-            gradient_batched<<<gc, kBlock, 0, st>>>(cases, WCFD_P, 2);
+            gradient_batched<<<gc, fb, 0, st>>>(cases, WCFD_P, 2);
             BCHECK("gradient_batched");
         }
     }

@@ -10,6 +10,7 @@
 namespace wcfd {
 
 constexpr int kBlock = 256;      // threads of the one-thread-per-face/cell kernels
+constexpr int kMaxFieldBlock = 512;  // largest block of the batched field kernels (a launch parameter)
 constexpr int kSolverBlock = 512;  // threads of the persistent Krylov kernels
 constexpr int kMaxSlots = 6;     // faces per cell (hex)
 constexpr int kClusterBlock = 1024;  // threads per CTA of the cluster-resident solver

@@ -20,15 +20,28 @@ namespace wcfd {
 __device__ __forceinline__ void face_pass_body(const wcfd_mesh& m, const wcfd_bc& bc, const wcfd_state& s, uint32_t mask, uint32_t flags, int k) {
     const int P = __ldg(m.face_owner + k);
     const int N = __ldg(m.face_nbr + k);
-    float4 fv = ld4(s.face_values + 4 * (size_t)k);
+    // an internal face with every field selected overwrites all four values: no read
+    float4 fv = (N >= 0 && mask == WCFD_ALL) ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : ld4(s.face_values + 4 * (size_t)k);
     const float4 cp = ld4(s.cell_values + 4 * (size_t)P);
     if (N >= 0) {
         const float4 gi = __ldg(reinterpret_cast<const float4*>(m.face_interp) + k);
         const float psi = gi.w;
         const float psi2 = 1.0f - psi;
         const float4 cn = ld4(s.cell_values + 4 * (size_t)N);
-        const float* gP = s.cell_gradients + 12 * (size_t)P;
-        const float* gN = s.cell_gradients + 12 * (size_t)N;
+        // every field: a cell's 4 x 3 gradients are 48 bytes, three 128-bit loads; a
+        // single field: only its three components
+        const float* gPp = s.cell_gradients + 12 * (size_t)P;
+        const float* gNp = s.cell_gradients + 12 * (size_t)N;
+        float gP[12], gN[12];
+        if ((flags & 4u) && mask == WCFD_ALL) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const float4 a = ld4(gPp + 4 * q);
+                const float4 b = ld4(gNp + 4 * q);
+                gP[4 * q] = a.x; gP[4 * q + 1] = a.y; gP[4 * q + 2] = a.z; gP[4 * q + 3] = a.w;
+                gN[4 * q] = b.x; gN[4 * q + 1] = b.y; gN[4 * q + 2] = b.z; gN[4 * q + 3] = b.w;
+            }
+        }
 #pragma unroll
         for (int o = 0; o < 4; ++o) {
             if (!(mask & (1u << o))) continue;
@@ -36,9 +49,14 @@ __device__ __forceinline__ void face_pass_body(const wcfd_mesh& m, const wcfd_bc
             if (flags & 8u) val = s.mass_fluxes[k] > 0.0f ? comp(cp, o) : comp(cn, o);
             else val = comp(cp, o) * psi + psi2 * comp(cn, o);
             if (flags & 4u) {
-                const float gx = gP[3 * o + 0] * psi + psi2 * gN[3 * o + 0];
-                const float gy = gP[3 * o + 1] * psi + psi2 * gN[3 * o + 1];
-                const float gz = gP[3 * o + 2] * psi + psi2 * gN[3 * o + 2];
+                const bool all = mask == WCFD_ALL;
+                const float px = all ? gP[3 * o] : gPp[3 * o], py = all ? gP[3 * o + 1] : gPp[3 * o + 1];
+                const float pz = all ? gP[3 * o + 2] : gPp[3 * o + 2];
+                const float nx = all ? gN[3 * o] : gNp[3 * o], ny = all ? gN[3 * o + 1] : gNp[3 * o + 1];
+                const float nz = all ? gN[3 * o + 2] : gNp[3 * o + 2];
+                const float gx = px * psi + psi2 * nx;
+                const float gy = py * psi + psi2 * ny;
+                const float gz = pz * psi + psi2 * nz;
                 val += gx * gi.x + gy * gi.y + gz * gi.z;
             }
             set_comp(fv, o, val);
@@ -226,44 +244,44 @@ __global__ void __launch_bounds__(kBlock) p_update_kernel(int C, const float* __
 // ---------------------------------------------------------------------------------
 // Batched forms: one launch for every case of a device case table; blockIdx.y is the
 // case, blockIdx.x runs over that case's faces or cells (blocks past the end of a smaller
-// case return at once).  The arithmetic is the single-case kernels' (same bodies).
+// case return at once).  The block size is a launch parameter (autotuned per batch).  The arithmetic is the single-case kernels' (same bodies).
 namespace wcfd {
 
-__global__ void __launch_bounds__(kBlock) face_pass_batched(const wcfd_case* __restrict__ cases, uint32_t mask,
+__global__ void __launch_bounds__(kMaxFieldBlock) face_pass_batched(const wcfd_case* __restrict__ cases, uint32_t mask,
                                                             uint32_t flags) {
     const wcfd_case& c = cases[blockIdx.y];
-    const int k = blockIdx.x * kBlock + threadIdx.x;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= c.mesh.n_faces) return;
     face_pass_body(c.mesh, c.bc, c.state, mask, flags | (c.prm.skew ? 4u : 0u), k);
 }
 
 // mode 0: gradients only; 1: + divergence into case.div; 2: + velocity correction
-__global__ void __launch_bounds__(kBlock) gradient_batched(const wcfd_case* __restrict__ cases, uint32_t mask,
+__global__ void __launch_bounds__(kMaxFieldBlock) gradient_batched(const wcfd_case* __restrict__ cases, uint32_t mask,
                                                            int mode) {
     const wcfd_case& c = cases[blockIdx.y];
-    const int i = blockIdx.x * kBlock + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.mesh.n_cells) return;
     const CorrectArgs corr{mode == 2 ? c.hbya : nullptr, c.rua};
     gradient_body(c.mesh, c.state, mask, mode == 1 ? c.div : nullptr, corr, i);
 }
 
-__global__ void __launch_bounds__(kBlock) hbya_batched(const wcfd_case* __restrict__ cases) {
+__global__ void __launch_bounds__(kMaxFieldBlock) hbya_batched(const wcfd_case* __restrict__ cases) {
     const wcfd_case& c = cases[blockIdx.y];
-    const int i = blockIdx.x * kBlock + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.mesh.n_cells) return;
     hbya_body(c.mesh.n_cells, c.state.cell_gradients, c.rua, c.hbya, c.state.cell_values, i);
 }
 
-__global__ void __launch_bounds__(kBlock) rua_faces_batched(const wcfd_case* __restrict__ cases) {
+__global__ void __launch_bounds__(kMaxFieldBlock) rua_faces_batched(const wcfd_case* __restrict__ cases) {
     const wcfd_case& c = cases[blockIdx.y];
-    const int k = blockIdx.x * kBlock + threadIdx.x;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= c.mesh.n_faces) return;
     cell_to_face_body(c.mesh, c.rua, c.rua_faces, k);
 }
 
-__global__ void __launch_bounds__(kBlock) p_update_batched(const wcfd_case* __restrict__ cases) {
+__global__ void __launch_bounds__(kMaxFieldBlock) p_update_batched(const wcfd_case* __restrict__ cases) {
     const wcfd_case& c = cases[blockIdx.y];
-    const int i = blockIdx.x * kBlock + threadIdx.x;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.mesh.n_cells) return;
     p_update_body(c.mesh.n_cells, c.p_x, c.state.cell_values, c.prm.steady ? c.prm.p_relax : 0.0f, i);
 }

@@ -9,17 +9,17 @@ from __future__ import annotations
 
 
 def cg_bytes_per_iteration(C: int, W: int) -> int:
-    """One CG iteration (three phases) per row:
-    q = A p      : off 4W + col 4W + diag 4 + p 4 + q(write) 4
-    x, r update  : x 8 + p 4 + r 8 + q 4 + invd 4
-    p update     : r 4 + invd 4 + p 8
+    """One CG iteration (two passes) per row:
+    p = z + beta p_old ; q = A p ; x += alpha_prev p_old :
+                   off 4W + col 4W + diag 4 + z 4 + p_old 4 + x 8 (rw) + p 4 (w) + q 4 (w)
+    r -= alpha q ; z = M r : r 8 (rw) + q 4 + invd 4 + z 4 (w)
     """
-    return C * (8 * W + 12 + 28 + 16)
+    return C * (8 * W + 28 + 20)
 
 
 def cg_bytes_setup(C: int, W: int) -> int:
-    """r = b - A x, invd, p: off/col 8W, diag 4, x 4, b 4, writes r, invd, p 12."""
-    return C * (8 * W + 24)
+    """r = b - A x, invd, z, p: off/col 8W, diag 4, x 4, b 4, writes r, invd, z, p 16."""
+    return C * (8 * W + 28)
 
 
 def cg_bytes(C: int, W: int, iters: int) -> int:
@@ -43,7 +43,9 @@ def bicgstab_bytes(C: int, W: int, iters: int) -> int:
 
 
 def face_pass_bytes(C: int, K: int, Ki: int, B: int, mdot: bool = True) -> int:
-    b = 8 * K + 16 * Ki + 32 * K + 64 * C          # owner/nbr, interp, face values rw, cell values+grads
+    """Every field: internal faces only write their values (16), boundary faces read and
+    write them (32) and their gradients."""
+    b = 8 * K + 16 * Ki + 16 * K + 16 * B + 64 * C  # owner/nbr, interp, face values, cell values+grads
     b += B * (4 + 4 + 16 + 32 + 4)                   # brow, bc type, bc value, face grads rw, rpf
     if mdot:
         b += 16 * K + 4 * K

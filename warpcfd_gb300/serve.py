@@ -230,7 +230,7 @@ class Server:
 
     def __init__(self, hbm_budget=16 << 30, max_active=256, tol=1e-6, check_every=10, max_outer=4000,
                  buckets=(4096, 8192, 16384, 32768, 65536), atol=SERVE_ATOL, rtol=SERVE_RTOL, device=None,
-                 clock=time.perf_counter, keep_fields=False):
+                 clock=time.perf_counter, keep_fields=False, autotune=True, use_graphs=False):
         self.budget = int(hbm_budget)
         self.max_active = int(max_active)
         self.tol = float(tol)
@@ -242,6 +242,8 @@ class Server:
         self.device = device or torch.device("cuda", torch.cuda.current_device())
         self.clock = clock
         self.meshes = MeshCache()
+        self.autotune = autotune
+        self.use_graphs = use_graphs
         self._geometry_charged = set()
         self._geometry_bytes = 0
         self.keep_fields = keep_fields
@@ -353,17 +355,24 @@ class Server:
                     batches[bi] = None
                 if not active[bi]:
                     continue
-                if batches[bi] is None:
-                    batches[bi] = CaseBatch([s.solver for s in active[bi]], cluster_size=self.cluster_sizes[bi])
                 stream = self.streams[bi]
                 stream.wait_stream(cur)  # uploads of newly admitted cases
+                if batches[bi] is None:
+                    batches[bi] = CaseBatch([s.solver for s in active[bi]], cluster_size=self.cluster_sizes[bi])
+                    if self.autotune:
+                        from .autotune import tune_field_block
+                        with torch.cuda.stream(stream):
+                            tune_field_block(batches[bi], key=("serve", self.bounds[bi], self.cluster_sizes[bi]))
                 host = torch.empty(batches[bi].stats.numel(), dtype=torch.uint8, pin_memory=True)
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 with torch.cuda.stream(stream):
                     e0.record(stream)
-                    for _ in range(self.check_every):
-                        batches[bi].step()
+                    if self.use_graphs:
+                        batches[bi].steps(self.check_every)
+                    else:
+                        for _ in range(self.check_every):
+                            batches[bi].step()
                     host.copy_(batches[bi].stats, non_blocking=True)
                     e1.record(stream)
                 inflight[bi] = (e0, e1, host)
