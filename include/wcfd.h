@@ -135,7 +135,7 @@ typedef struct wcfd_params {
     double  atol_u;         /* momentum BiCGSTAB absolute tolerance               */
     double  atol_p;         /* pressure CG absolute tolerance                     */
     int32_t p_refine;       /* fp64 iterative-refinement sweeps of the pressure solve; 0 = off */
-    int32_t pad_;
+    int32_t rhie_chow;      /* 1 = Rhie-Chow convecting flux (opt-in; the reference's path is 0) */
     double  p_refine_rtol;  /* relative tolerance of each sweep's fp32 CG correction solve */
     double  rtol_u;         /* momentum stop also at ||r|| <= rtol_u ||r_0||; 0 = atol only (the reference) */
     double  rtol_p;         /* pressure stop also at ||r|| <= rtol_p ||r_0||; 0 = atol only (the reference) */

@@ -405,3 +405,28 @@ def test_device_convergence_monitor_matches_reference_norms():
         assert abs(got - want) <= tol * max(abs(want), 1e-30) + 1e-12, (k, got, want)
     conv, _ = model.check_convergence_norms(norms)
     assert set(conv) >= {"momentum_x", "continuity", "velocity_correction", "pressure_correction"}
+
+
+@pytest.mark.parametrize("case", ["cavity_skew", "channel"])
+def test_rhie_chow_option_tracks_oracle(case):
+    """Opt-in Rhie-Chow convecting flux (IncompressibleSolver.rhie_chow): the GPU follows the
+    oracle's restatement of the same option step by step."""
+    mk = {"cavity_skew": (lambda: cavity_mesh(16, jitter=0.15, seed=11), cavity_bc, 0, 0.01),
+          "channel": (lambda: channel_mesh(40, 8), channel_bc, None, 0.05)}[case]
+    model, solver, oc = make_pair(mk[0](), mk[1], ref_cell=mk[2], nu=mk[3])
+    solver.rhie_chow = True
+    oc.rhie_chow = True
+    for it in range(5):
+        solver.step()
+        oracle_step(oc)
+        g = fields(model)
+        tol_u = 1e-5 if it == 0 else 1e-4
+        tol_p = 1e-4 if it == 0 else 1e-3
+        for o in range(3):
+            assert vel_err(g, oc.cell_values, o) < tol_u, (it, o)
+        assert rel_l2(g[:, 3], oc.cell_values[:, 3]) < tol_p, it
+    # the option changes the flux from the second iteration on (rUA_f is zero before)
+    m2, s2, _ = make_pair(mk[0](), mk[1], ref_cell=mk[2], nu=mk[3])
+    for _ in range(5):
+        s2.step()
+    assert not torch.equal(model.cell_values, m2.cell_values)

@@ -58,6 +58,9 @@ class IncompressibleSolver:
         # precision form: fp64 iterative refinement of the pressure solve (0 = off)
         self.p_refine = 0
         self.p_refine_rtol = 1e-3
+        # opt-in Rhie-Chow convecting flux (the reference re-interpolates the flux from the
+        # corrected cell velocities, incompressible.py:97-99)
+        self.rhie_chow = False
         self.p_x64 = None
         self.p_work = None
         self._graph = None
@@ -100,7 +103,8 @@ class IncompressibleSolver:
                              -1 if ref is None else int(ref), int(steady), int(self.NUM_INNER_LOOPS),
                              int(self.NUM_ORTHOGONAL_CORRECTORS), int(self.vel_equation.max_iter),
                              int(bool(m.skew_correction)), float(self.vel_equation.tol),
-                             float(self.p_corr_equation.tol), int(self.p_refine), 0, float(self.p_refine_rtol),
+                             float(self.p_corr_equation.tol), int(self.p_refine), int(bool(self.rhie_chow)),
+                             float(self.p_refine_rtol),
                              float(self.vel_equation.rtol), float(self.p_corr_equation.rtol))
 
     def _param_key(self):
@@ -109,7 +113,7 @@ class IncompressibleSolver:
                 self.p_relaxation_factor, self.dt, m.reference_pressure_cell_id, m.reference_pressure,
                 self.NUM_INNER_LOOPS, self.NUM_ORTHOGONAL_CORRECTORS, self.vel_equation.max_iter,
                 m.skew_correction, self.vel_equation.tol, self.p_corr_equation.tol, self._events_ptr,
-                self.p_refine, self.p_refine_rtol, self.vel_equation.rtol, self.p_corr_equation.rtol)
+                self.p_refine, self.p_refine_rtol, self.vel_equation.rtol, self.p_corr_equation.rtol, self.rhie_chow)
 
     def case_struct(self) -> _lib.Case_t:
         """The C struct of this case; rebuilt only when a parameter changed (the device

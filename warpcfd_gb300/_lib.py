@@ -71,7 +71,7 @@ class Params_t(ct.Structure):
     _fields_ = [("nu", ct.c_float), ("rho", ct.c_float), ("u_relax", ct.c_float), ("p_relax", ct.c_float),
                 ("dt", ct.c_float), ("ref_value", ct.c_float), ("ref_cell", ct.c_int32), ("steady", ct.c_int32),
                 ("n_inner", ct.c_int32), ("n_ortho", ct.c_int32), ("maxiter", ct.c_int32), ("skew", ct.c_int32),
-                ("atol_u", ct.c_double), ("atol_p", ct.c_double), ("p_refine", ct.c_int32), ("pad_", ct.c_int32),
+                ("atol_u", ct.c_double), ("atol_p", ct.c_double), ("p_refine", ct.c_int32), ("rhie_chow", ct.c_int32),
                 ("p_refine_rtol", ct.c_double), ("rtol_u", ct.c_double), ("rtol_p", ct.c_double)]
 
 

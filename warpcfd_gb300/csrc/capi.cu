@@ -241,7 +241,7 @@ int wcfd_face_pass_flags(const wcfd_mesh* m, wcfd_bc bc, wcfd_state s, uint32_t 
     RET_IF(!bc.type || !bc.value || !s.cell_values || !s.cell_gradients || !s.face_values || !s.face_gradients ||
                !s.mass_fluxes,
            WCFD_ERR_ARGUMENT, "null field");
-    face_pass_kernel<<<grid_for(m->n_faces), kBlock, 0, S(stream)>>>(*m, bc, s, mask, flags);
+    face_pass_kernel<<<grid_for(m->n_faces), kBlock, 0, S(stream)>>>(*m, bc, s, mask, flags & 15u, nullptr);
     LAUNCH_CHECK("face_pass_kernel");
     return WCFD_OK;
 }
@@ -408,7 +408,8 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
     const uint32_t skew = c.prm.skew ? 4u : 0u;
     const int gf = grid_for(m.n_faces), gc = grid_for(m.n_cells);
     // incompressible.py:96-99
-    face_pass_kernel<<<gf, kBlock, 0, st>>>(m, c.bc, c.state, WCFD_ALL, 1u | 2u | skew);
+    face_pass_kernel<<<gf, kBlock, 0, st>>>(m, c.bc, c.state, WCFD_ALL, 1u | 2u | skew | (c.prm.rhie_chow ? 16u : 0u),
+                                            c.rua_faces);
     LAUNCH_CHECK("face_pass_kernel");
     gradient_kernel<<<gc, kBlock, 0, st>>>(m, c.state, WCFD_ALL, nullptr, CorrectArgs{nullptr, nullptr});
     LAUNCH_CHECK("gradient_kernel");
@@ -430,7 +431,7 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
     for (int inner = 0; inner < c.prm.n_inner; ++inner) {
         for (int ortho = 0; ortho < c.prm.n_ortho; ++ortho) {
             // :127-132
-            face_pass_kernel<<<gf, kBlock, 0, st>>>(m, c.bc, c.state, WCFD_ALL, 2u | skew);
+            face_pass_kernel<<<gf, kBlock, 0, st>>>(m, c.bc, c.state, WCFD_ALL, 2u | skew, nullptr);
             LAUNCH_CHECK("face_pass_kernel");
             gradient_kernel<<<gc, kBlock, 0, st>>>(m, c.state, WCFD_ALL, c.div, CorrectArgs{nullptr, nullptr});
             LAUNCH_CHECK("gradient_kernel");
@@ -451,7 +452,7 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
                                                    c.prm.steady ? c.prm.p_relax : 0.0f);
             LAUNCH_CHECK("p_update_kernel");
             // :150-156
-            face_pass_kernel<<<gf, kBlock, 0, st>>>(m, c.bc, c.state, WCFD_P, skew);
+            face_pass_kernel<<<gf, kBlock, 0, st>>>(m, c.bc, c.state, WCFD_P, skew, nullptr);
             LAUNCH_CHECK("face_pass_kernel");
             gradient_kernel<<<gc, kBlock, 0, st>>>(m, c.state, WCFD_P, nullptr, CorrectArgs{c.hbya, c.rua});
             LAUNCH_CHECK("gradient_kernel");

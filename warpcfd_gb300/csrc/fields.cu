@@ -16,8 +16,14 @@ namespace wcfd {
 // flags: bit0 apply every field's boundary table first (set_boundary_conditions),
 //        bit1 recompute the mass flux, bit2 skew correction, bit3 upwind instead of
 //        linear interpolation on internal faces (phi_P if mdot > 0 else phi_N,
-//        interpolation_functions.py:18-28; used by face_interpolation(upwind=True)).
-__device__ __forceinline__ void face_pass_body(const wcfd_mesh& m, const wcfd_bc& bc, const wcfd_state& s, uint32_t mask, uint32_t flags, int k) {
+//        interpolation_functions.py:18-28; used by face_interpolation(upwind=True)),
+//        bit4 (opt-in, not the reference's path) Rhie-Chow flux on internal faces:
+//        mdot = u_f . n A - rUA_f (gdiff (p_N - p_P) - (psi grad p_P + (1-psi) grad p_N) . n A)
+//        with the pressure equation's own compact coefficient gdiff, so the convecting flux is
+//        the pressure equation's face flux (the form of FV/_deprecated/mesh_ops.py:59-93,
+//        written with the full owner-to-neighbour distance); rua_f may be null otherwise.
+__device__ __forceinline__ void face_pass_body(const wcfd_mesh& m, const wcfd_bc& bc, const wcfd_state& s, uint32_t mask, uint32_t flags, int k,
+                                               const float* __restrict__ rua_f = nullptr) {
     const int P = __ldg(m.face_owner + k);
     const int N = __ldg(m.face_nbr + k);
     // an internal face with every field selected overwrites all four values: no read
@@ -84,15 +90,26 @@ __device__ __forceinline__ void face_pass_body(const wcfd_mesh& m, const wcfd_bc
     st4(s.face_values + 4 * (size_t)k, fv);
     if (flags & 2u) {
         const float4 n = __ldg(reinterpret_cast<const float4*>(m.face_normal) + k);
-        s.mass_fluxes[k] = (fv.x * n.x + fv.y * n.y + fv.z * n.z) * n.w;
+        float md = (fv.x * n.x + fv.y * n.y + fv.z * n.z) * n.w;
+        if ((flags & 16u) && rua_f && N >= 0) {
+            const float4 gi = __ldg(reinterpret_cast<const float4*>(m.face_interp) + k);
+            const float psi = gi.w, psi2 = 1.0f - psi;
+            const float4 cn = ld4(s.cell_values + 4 * (size_t)N);
+            const float* gP = s.cell_gradients + 12 * (size_t)P + 9;
+            const float* gN = s.cell_gradients + 12 * (size_t)N + 9;
+            const float gn = (gP[0] * psi + psi2 * gN[0]) * n.x + (gP[1] * psi + psi2 * gN[1]) * n.y +
+                             (gP[2] * psi + psi2 * gN[2]) * n.z;
+            md -= rua_f[k] * (__ldg(m.face_gdiff + k) * (cn.w - cp.w) - gn * n.w);
+        }
+        s.mass_fluxes[k] = md;
     }
 }
 
 __global__ void __launch_bounds__(kBlock) face_pass_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s,
-                                                           uint32_t mask, uint32_t flags) {
+                                                           uint32_t mask, uint32_t flags, const float* rua_f) {
     const int k = blockIdx.x * kBlock + threadIdx.x;
     if (k >= m.n_faces) return;
-    face_pass_body(m, bc, s, mask, flags, k);
+    face_pass_body(m, bc, s, mask, flags, k, rua_f);
 }
 
 // Green-Gauss gradient (model.py:232-239, model_kernels.py:71-90):
@@ -252,7 +269,10 @@ __global__ void __launch_bounds__(kMaxFieldBlock) face_pass_batched(const wcfd_c
     const wcfd_case& c = cases[blockIdx.y];
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= c.mesh.n_faces) return;
-    face_pass_body(c.mesh, c.bc, c.state, mask, flags | (c.prm.skew ? 4u : 0u), k);
+    // the Rhie-Chow option applies to the convecting flux, formed by the pass that also
+    // applies the boundary values (the first of an outer iteration)
+    const uint32_t rc = (c.prm.rhie_chow && (flags & 1u)) ? 16u : 0u;
+    face_pass_body(c.mesh, c.bc, c.state, mask, flags | rc | (c.prm.skew ? 4u : 0u), k, c.rua_faces);
 }
 
 // mode 0: gradients only; 1: + divergence into case.div; 2: + velocity correction
