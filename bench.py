@@ -285,34 +285,55 @@ def run_reference(args):
 
 def run_serve(args):
     """Serving mix through the continuous-batching server; the drop-in path (one case at a
-    time, same settings) runs a bounded sample of the same mix for the comparison."""
+    time, same settings) runs a bounded sample of the same mix for the comparison.  Under
+    torchrun each rank serves its round-robin share of the mix on its own GPU (replicas, no
+    collective on the data path); rank 0 prints the whole-job figures."""
     import torch
 
     from warpcfd_gb300.build import build_library
+    from warpcfd_gb300.replicas import max_over_ranks, shard, sum_over_ranks
     from warpcfd_gb300.serve import Server, make_request_mix, run_drop_in
 
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     build_library()
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    reqs = make_request_mix(args.requests, seed=0, rate=args.rate)
-    # warm-up: a few small requests compile nothing but touch every kernel and the caches
+    reqs_all = make_request_mix(args.requests, seed=0, rate=args.rate)
+    reqs = shard(reqs_all, rank, world)
+    # warm-up: a few small requests touch every kernel and the caches
     Server(max_outer=30).run(make_request_mix(4, seed=1, rate=1e6, lo=32 * 32, hi=48 * 48))
     torch.cuda.synchronize()
-    with ClockSampler(0, enabled=not args.no_clocks) as clocks:
+    if dist is not None:
+        dist.barrier()
+    with ClockSampler(local, enabled=not args.no_clocks) as clocks:
         rep = Server(max_outer=args.max_outer).run(reqs)
     summ = rep.summary()
-    # drop-in on a sample: the first requests in arrival order, same stop settings
+    wall = max_over_ranks(summ["wall_s"])
+    cell_its = sum_over_ranks(rep.cell_iterations)
+    value = cell_its / wall
+    # drop-in on a sample: the first requests of this rank's share, same stop settings
     n_drop = min(args.drop_in_sample, len(reqs))
     drop = run_drop_in(reqs[:n_drop], max_outer=args.max_outer)
+    drop_rate = sum_over_ranks(drop["cell_iterations_per_s"]) / world
+    if dist is not None:
+        dist.destroy_process_group()
+    if rank != 0:
+        return 0
     line = {
-        "metric": METRIC, "value": summ["cell_iterations_per_s"], "unit": METRIC, "n_gpus": 1, "steps": len(reqs),
-        "warmup": 4, "ms_per_step": 1e3 * summ["wall_s"] / max(len(reqs), 1), "higher_is_better": True,
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": len(reqs_all),
+        "warmup": 4, "ms_per_step": 1e3 * wall / max(len(reqs_all), 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOADS["serve"], "requests": len(reqs), "arrival_rate_per_s": args.rate,
-                   "max_outer": args.max_outer, "step": "one request served to completion"},
+        "config": {"workload": WORKLOADS["serve"], "requests": len(reqs_all), "arrival_rate_per_s": args.rate,
+                   "max_outer": args.max_outer, "step": "one request served to completion",
+                   "parallelism": f"request shards x{world}"},
         "serving": summ,
-        "drop_in": {"requests": n_drop, "cell_iterations_per_s": drop["cell_iterations_per_s"],
-                    "wall_s": drop["wall_s"]},
-        "batched_over_drop_in": summ["cell_iterations_per_s"] / max(drop["cell_iterations_per_s"], 1e-9),
+        "drop_in": {"requests_per_rank": n_drop, "cell_iterations_per_s": drop_rate, "wall_s": drop["wall_s"]},
+        "batched_over_drop_in": value / world / max(drop_rate, 1e-9),
         "clocks": clocks.summary(),
     }
     print(json.dumps(line))
@@ -381,12 +402,9 @@ def run_ours(args):
     if not finite:
         raise SystemExit("bench: the fields went non-finite during the timed steps; no valid measurement")
     rel_res = hist[:, 0]["initial_residual"] / np.maximum(hist[:, 0]["rhs_norm"], 1e-300)
-    total_ms = float(step_ms.sum())
-    if dist is not None:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * C * K_ / (total_ms * 1e-3)
+    from warpcfd_gb300.replicas import job_throughput, max_over_ranks
+    total_ms = max_over_ranks(float(step_ms.sum()))
+    value = job_throughput(C * K_, world, total_ms * 1e-3)
 
     # end to end through the public API with host buffers (H2D inputs, D2H result per step):
     # the same K steps again from the post-warm-up snapshot (the path is bitwise
