@@ -430,3 +430,33 @@ def test_rhie_chow_option_tracks_oracle(case):
     for _ in range(5):
         s2.step()
     assert not torch.equal(model.cell_values, m2.cell_values)
+
+
+def test_cluster_cg_at_its_size_limit():
+    """The cluster-resident CG at the largest system its 16 CTAs hold (65,536 rows of width
+    4, 4,096 rows per CTA, 4 rows per thread) and one row past it (the solve falls back to
+    the grid-cooperative kernel) agree with the grid kernel on the same systems."""
+    from warpcfd_gb300 import _lib
+
+    lib = _lib.load()
+    rows = int(lib.wcfd_batch_max_rows(4))
+    assert rows == 4096
+    for n, m_ in ((256, 256), (257, 256)):
+        mesh = cavity_mesh(n) if n == m_ else channel_mesh(n, m_, lx=float(n) / m_)
+        bc = cavity_bc if n == m_ else channel_bc
+        model, solver, _ = make_pair(mesh, bc, ref_cell=0 if n == m_ else None)
+        solver.step()
+        torch.cuda.synchronize()
+        pe = solver.p_corr_equation
+        out = {}
+        try:
+            for path in (1, 2):
+                assert lib.wcfd_set_krylov_path(path) == 0
+                x = torch.zeros_like(pe.x)
+                pe.tol, pe.max_iter = 1e-7, 400
+                st, _ = pe.solve_Axb(x)
+                out[path] = (x.cpu().numpy(), st)
+        finally:
+            lib.wcfd_set_krylov_path(0)
+        assert abs(out[1][1]["iterations"] - out[2][1]["iterations"]) <= max(2, out[1][1]["iterations"] // 50), (n, out)
+        assert rel_l2(out[1][0], out[2][0]) < 1e-4, n

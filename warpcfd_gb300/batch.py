@@ -20,7 +20,9 @@ from . import _lib
 class CaseBatch:
     """``cluster_size``: CTAs per case for the Krylov solves (0 = the library's pick);
     ``field_block``: threads per block of the field and assembly kernels (0 = 256; see
-    warpcfd_gb300.autotune)."""
+    warpcfd_gb300.autotune).  The device case table is uploaded on the stream current at
+    construction (and at refresh()); a caller that steps the batch on another stream must
+    first make that stream wait for this one."""
 
     def __init__(self, solvers, cluster_size: int = 0, device=None, field_block: int = 0):
         if not solvers:

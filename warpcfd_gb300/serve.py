@@ -356,13 +356,16 @@ class Server:
                 if not active[bi]:
                     continue
                 stream = self.streams[bi]
-                stream.wait_stream(cur)  # uploads of newly admitted cases
-                if batches[bi] is None:
+                fresh = batches[bi] is None
+                if fresh:
+                    # the case table is uploaded on the current stream
                     batches[bi] = CaseBatch([s.solver for s in active[bi]], cluster_size=self.cluster_sizes[bi])
-                    if self.autotune:
-                        from .autotune import tune_field_block
-                        with torch.cuda.stream(stream):
-                            tune_field_block(batches[bi], key=("serve", self.bounds[bi], self.cluster_sizes[bi]))
+                # the bucket's stream runs after the uploads of admitted cases and the table
+                stream.wait_stream(cur)
+                if fresh and self.autotune:
+                    from .autotune import tune_field_block
+                    with torch.cuda.stream(stream):
+                        tune_field_block(batches[bi], key=("serve", self.bounds[bi], self.cluster_sizes[bi]))
                 host = torch.empty(batches[bi].stats.numel(), dtype=torch.uint8, pin_memory=True)
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
