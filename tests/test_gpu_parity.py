@@ -255,7 +255,7 @@ def test_cg_paths_agree_with_oracle(case):
 
 
 def test_cylinder_piso_with_correction_tracks_oracle():
-    """configs[2] in small: jittered all-hex O-grid around a cylinder, parabolic inlet,
+    """The cylinder-in-channel PISO case, small: jittered all-hex O-grid around a cylinder, parabolic inlet,
     PISO with 2 correctors and the non-orthogonal Laplacian correction."""
     from warpcfd_gb300.preprocess import (Mesh, create_cylinder_channel_grid, define_boundary_walls,
                                           define_cylinder_group)
