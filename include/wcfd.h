@@ -215,6 +215,16 @@ int wcfd_assemble_momentum(const wcfd_case* c, void* stream);
  * row (incompressible.py:132-140, equation_kernels.py:155-175). */
 int wcfd_assemble_pressure(const wcfd_case* c, void* stream);
 
+/* Implicit relaxation of an assembled system (Equation.relax, equation.py:173-182;
+ * equation_kernels.py:128-152): b += (1 - alpha)/alpha d phi and d /= alpha on every
+ * diagonal entry, phi the row's field in the C x 4 cell values (fields field0 ..
+ * field0 + ncomp - 1).  alpha in (0, 1]. */
+int wcfd_relax(const wcfd_mesh* m, wcfd_system A, const float* cell_values, int32_t field0, float alpha,
+               void* stream);
+/* Row `row` of a scalar system becomes the identity with rhs = value (Equation.replace_row,
+ * equation.py:185-194; equation_kernels.py:155-175). */
+int wcfd_replace_row(const wcfd_mesh* m, wcfd_system A, int32_t row, float value, void* stream);
+
 /* y = A x on the mesh pattern (warp.sparse.bsr_mv; model.py:287). */
 int wcfd_spmv(const wcfd_mesh* m, wcfd_system A, const float* x, float* y, void* stream);
 

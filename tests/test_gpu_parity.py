@@ -460,3 +460,51 @@ def test_cluster_cg_at_its_size_limit():
             lib.wcfd_set_krylov_path(0)
         assert abs(out[1][1]["iterations"] - out[2][1]["iterations"]) <= max(2, out[1][1]["iterations"] // 50), (n, out)
         assert rel_l2(out[1][0], out[2][0]) < 1e-4, n
+
+
+@pytest.mark.parametrize("steady", [True, False])
+def test_term_equation_api_matches_fused_assembly(steady):
+    """The reference's Term/Equation API (form_system, relax, add_RHS, replace_row) builds the
+    same momentum and pressure systems, bit for bit, as the fused solver assembly."""
+    m = cavity_mesh(12, jitter=0.1, seed=6)
+    model, solver, oc = make_pair(m, cavity_bc, steady=steady, dt=0.01)
+    _seed_state(model, oc, 7)
+    model.set_boundary_conditions()
+    model.face_interpolation()
+    model.calculate_gradients()
+    model.calculate_mass_flux()
+    solver.assemble_momentum()                 # fused: terms, relaxation (steady) and rUA
+    ve = solver.vel_equation
+    fused = [t.clone() for t in (ve.diag, ve.off, ve.rhs)]
+    ve.diag.zero_(), ve.off.zero_(), ve.rhs.zero_()
+    nu = float(model.material.viscosity) / float(model.material.density)
+    solver.convection(model)
+    solver.diffusion(model, viscosity=nu)
+    solver.grad_P(model)
+    inv_density = 1.0 / float(model.material.density)
+    if steady:
+        ve.form_system([solver.convection, -solver.diffusion], explicit_terms=-inv_density * solver.grad_P, fvm=model)
+        ve.relax(solver.u_relaxation_factor, model)
+    else:
+        solver.ddt(model, dt=0.01)
+        ve.form_system([solver.ddt, solver.convection, -solver.diffusion],
+                       explicit_terms=-inv_density * solver.grad_P, fvm=model)
+    torch.cuda.synchronize()
+    for a, b in zip(fused, (ve.diag, ve.off, ve.rhs)):
+        assert torch.equal(a, b)
+    # pressure: form_system + add_RHS(div) + replace_row, against the fused pressure assembly
+    rua_f = torch.rand(m.num_faces, device="cuda") + 0.1
+    solver.rUA_faces.copy_(rua_f)
+    div = torch.randn(m.num_cells, device="cuda")
+    solver.div_u.copy_(div)
+    solver.assemble_pressure()
+    pe = solver.p_corr_equation
+    fused = [t.clone() for t in (pe.diag, pe.off, pe.rhs)]
+    pe.diag.zero_(), pe.off.zero_(), pe.rhs.zero_()
+    solver.p_correction_diffusion(model, viscosity=rua_f)
+    pe.form_system(solver.p_correction_diffusion, fvm=model)
+    pe.add_RHS(div)
+    pe.replace_row(model.reference_pressure_cell_id, float(model.reference_pressure))
+    torch.cuda.synchronize()
+    for a, b in zip(fused, (pe.diag, pe.off, pe.rhs)):
+        assert torch.allclose(a, b, rtol=0, atol=0) or torch.equal(a, b)

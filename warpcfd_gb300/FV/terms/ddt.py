@@ -9,3 +9,10 @@ class DdtTerm(Term):
         if time_scheme != "backwardEuler":
             raise NotImplementedError("Only backwardEuler valid option now")
         self.time_scheme = time_scheme
+        self.dt = None
+
+    def calculate_weights(self, fv, dt=None, **kwargs):
+        """Records the time step of the next form_system (ddt.py:24-32)."""
+        if dt is not None:
+            self.dt = float(dt)
+        return self

@@ -15,3 +15,11 @@ class DiffusionTerm(Term):
         self.correction = correction
         self.von_neumann = von_neumann
         self.dirchlet = dirchlet
+        self.viscosity = None
+
+    def calculate_weights(self, fv, viscosity=None, **kwargs):
+        """Records the viscosity of the next form_system: a scalar, or a tensor of one value
+        per face (diffusion.py:113-198 forms the weights here; the assembly kernels do)."""
+        if viscosity is not None:
+            self.viscosity = viscosity
+        return self

@@ -106,6 +106,33 @@ __global__ void __launch_bounds__(kBlock) momentum_assemble_kernel(wcfd_mesh m, 
     momentum_assemble_body(m, bc, s, sys, rua, prm, c);
 }
 
+// Implicit relaxation of an assembled system on its diagonal (equation_kernels.py:128-152):
+// b += (1 - a)/a d phi ; d /= a, phi the cell value of the row's field (fields field0 ..
+// field0 + ncomp - 1 of the C x 4 cell values).  The same expression as the relaxation
+// inside momentum_assemble_body, so the two routes give the same bits.
+__global__ void __launch_bounds__(kBlock) relax_kernel(int C, wcfd_system sys, const float* __restrict__ cell_values,
+                                                       int field0, float a) {
+    const int c = blockIdx.x * kBlock + threadIdx.x;
+    if (c >= C) return;
+    for (int o = 0; o < sys.ncomp; ++o) {
+        const size_t r = (size_t)sys.ncomp * c + o;
+        const float d = sys.diag[r];
+        sys.rhs[r] += (1.0f - a) / a * d * cell_values[4 * (size_t)c + field0 + o];
+        sys.diag[r] = d / a;
+    }
+}
+
+// Row `row` of a scalar system becomes the identity with rhs = value
+// (equation_kernels.py:155-175); its column is left as it is.
+__global__ void replace_row_kernel(int C, int W, wcfd_system sys, int row, float value) {
+    const int j = threadIdx.x;
+    if (j < W) sys.off[(size_t)j * C + row] = 0.0f;
+    if (j == 0) {
+        sys.diag[row] = 1.0f;
+        sys.rhs[row] = value;
+    }
+}
+
 // Pressure row of cell c: DiffusionTerm('p', nu = rUA_f), scale +1 (diffusion.py:113-198)
 //   internal:          diag -= rUA_f A/d ; off = +rUA_f A/d
 //   boundary value:    diag -= rUA_f A/|r_Pf| ; rhs -= rUA_f A/|r_Pf| p_b

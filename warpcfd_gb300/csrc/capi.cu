@@ -317,6 +317,28 @@ int wcfd_assemble_pressure(const wcfd_case* c, void* stream) {
     return WCFD_OK;
 }
 
+int wcfd_relax(const wcfd_mesh* m, wcfd_system A, const float* cell_values, int32_t field0, float alpha,
+               void* stream) {
+    int rc = check_mesh(m);
+    if (rc) return rc;
+    RET_IF(!A.diag || !A.rhs || !cell_values || (A.ncomp != 1 && A.ncomp != 3), WCFD_ERR_ARGUMENT, "bad system");
+    RET_IF(field0 < 0 || field0 + A.ncomp > 4, WCFD_ERR_ARGUMENT, "fields out of range");
+    RET_IF(!(alpha > 0.0f && alpha <= 1.0f), WCFD_ERR_ARGUMENT, "relaxation factor must be in (0, 1]");
+    relax_kernel<<<grid_for(m->n_cells), kBlock, 0, S(stream)>>>(m->n_cells, A, cell_values, field0, alpha);
+    LAUNCH_CHECK("relax_kernel");
+    return WCFD_OK;
+}
+
+int wcfd_replace_row(const wcfd_mesh* m, wcfd_system A, int32_t row, float value, void* stream) {
+    int rc = check_mesh(m);
+    if (rc) return rc;
+    RET_IF(!A.diag || !A.off || !A.rhs || A.ncomp != 1, WCFD_ERR_ARGUMENT, "replace_row takes a scalar system");
+    RET_IF(row < 0 || row >= m->n_cells, WCFD_ERR_ARGUMENT, "row out of range");
+    replace_row_kernel<<<1, 32, 0, S(stream)>>>(m->n_cells, m->ell_width, A, row, value);
+    LAUNCH_CHECK("replace_row_kernel");
+    return WCFD_OK;
+}
+
 int wcfd_spmv(const wcfd_mesh* m, wcfd_system A, const float* x, float* y, void* stream) {
     int rc = check_mesh(m);
     if (rc) return rc;
