@@ -215,6 +215,12 @@ int wcfd_assemble_momentum(const wcfd_case* c, void* stream);
  * row (incompressible.py:132-140, equation_kernels.py:155-175). */
 int wcfd_assemble_pressure(const wcfd_case* c, void* stream);
 
+/* rUA = V / (a_P rho) from the 3C interleaved momentum diagonal (calculate_rUA,
+ * solver_kernels.py:6-16). */
+int wcfd_rua(const wcfd_mesh* m, const float* diag3, float rho, float* rua, void* stream);
+/* HbyA += rUA grad p, 3C interleaved rows (get_HbyA, solver_kernels.py:38-43). */
+int wcfd_hbya_add(int32_t n_cells, const float* pgrad3, const float* rua, float* hbya, void* stream);
+
 /* Implicit relaxation of an assembled system (Equation.relax, equation.py:173-182;
  * equation_kernels.py:128-152): b += (1 - alpha)/alpha d phi and d /= alpha on every
  * diagonal entry, phi the row's field in the C x 4 cell values (fields field0 ..

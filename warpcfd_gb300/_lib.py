@@ -106,6 +106,8 @@ _SIGS = {
     "wcfd_spmv": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, vp, vp]),
     "wcfd_cg": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, KrylovWS_t, ct.c_double, ct.c_int32, vp, vp]),
     "wcfd_bicgstab": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, KrylovWS_t, ct.c_double, ct.c_int32, vp, vp]),
+    "wcfd_rua": (ct.c_int, [ct.POINTER(Mesh_t), vp, ct.c_float, vp, vp]),
+    "wcfd_hbya_add": (ct.c_int, [ct.c_int32, vp, vp, vp, vp]),
     "wcfd_relax": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, ct.c_int32, ct.c_float, vp]),
     "wcfd_replace_row": (ct.c_int, [ct.POINTER(Mesh_t), System_t, ct.c_int32, ct.c_float, vp]),
     "wcfd_krylov_solve": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, KrylovWS_t, ct.c_int32, ct.c_double,

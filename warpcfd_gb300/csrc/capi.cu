@@ -292,6 +292,22 @@ int wcfd_cell_to_face(const wcfd_mesh* m, const float* cell, float* face, void* 
     return WCFD_OK;
 }
 
+int wcfd_rua(const wcfd_mesh* m, const float* diag3, float rho, float* rua, void* stream) {
+    int rc = check_mesh(m);
+    if (rc) return rc;
+    RET_IF(!diag3 || !rua || rho == 0.0f, WCFD_ERR_ARGUMENT, "null array or zero density");
+    rua_kernel<<<grid_for(m->n_cells), kBlock, 0, S(stream)>>>(m->n_cells, m->cell_volume, diag3, rho, rua);
+    LAUNCH_CHECK("rua_kernel");
+    return WCFD_OK;
+}
+
+int wcfd_hbya_add(int32_t n_cells, const float* pgrad3, const float* rua, float* hbya, void* stream) {
+    RET_IF(n_cells <= 0 || !pgrad3 || !rua || !hbya, WCFD_ERR_ARGUMENT, "bad arguments");
+    hbya_add_kernel<<<grid_for(n_cells), kBlock, 0, S(stream)>>>(n_cells, pgrad3, rua, hbya);
+    LAUNCH_CHECK("hbya_add_kernel");
+    return WCFD_OK;
+}
+
 int wcfd_assemble_momentum(const wcfd_case* c, void* stream) {
     RET_IF(!c, WCFD_ERR_ARGUMENT, "case is null");
     int rc = check_mesh(&c->mesh);

@@ -242,6 +242,26 @@ __global__ void __launch_bounds__(kBlock) hbya_kernel(int C, const float* __rest
     hbya_body(C, grad, rua, hbya, cell_values, c);
 }
 
+// rUA = V / (a_P rho) from the u-row diagonal (solver_kernels.py:6-16), the expression of
+// the fused momentum assembly
+__global__ void __launch_bounds__(kBlock) rua_kernel(int C, const float* __restrict__ vol, const float* __restrict__ diag3,
+                                                     float rho, float* __restrict__ rua) {
+    const int c = blockIdx.x * kBlock + threadIdx.x;
+    if (c >= C) return;
+    rua[c] = vol[c] / (diag3[3 * (size_t)c] * rho);
+}
+
+// HbyA += rUA grad p on 3C interleaved rows (solver_kernels.py:38-43), the expression of
+// hbya_body
+__global__ void __launch_bounds__(kBlock) hbya_add_kernel(int C, const float* __restrict__ pgrad3,
+                                                          const float* __restrict__ rua, float* __restrict__ hbya) {
+    const int c = blockIdx.x * kBlock + threadIdx.x;
+    if (c >= C) return;
+    const float r = rua[c];
+#pragma unroll
+    for (int o = 0; o < 3; ++o) hbya[3 * (size_t)c + o] = hbya[3 * (size_t)c + o] + pgrad3[3 * (size_t)c + o] * r;
+}
+
 // p = alpha p_new + (1 - alpha) p (model.py:381-384), or p = p_new (alpha <= 0).
 __device__ __forceinline__ void p_update_body(int C, const float* __restrict__ p_new, float* __restrict__ cell_values, float alpha, int c) {
     float* p = cell_values + 4 * (size_t)c + 3;

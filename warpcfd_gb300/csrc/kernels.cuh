@@ -36,6 +36,8 @@ __global__ void pressure_assemble_batched(const wcfd_case* cases);
 // y = A x (NC = A.ncomp), launched from assemble.cu where the kernel template lives
 __global__ void relax_kernel(int C, wcfd_system sys, const float* cell_values, int field0, float a);
 __global__ void replace_row_kernel(int C, int W, wcfd_system sys, int row, float value);
+__global__ void rua_kernel(int C, const float* vol, const float* diag3, float rho, float* rua);
+__global__ void hbya_add_kernel(int C, const float* pgrad3, const float* rua, float* hbya);
 void launch_spmv(const wcfd_mesh& m, wcfd_system A, const float* x, float* y, cudaStream_t st);
 
 // persistent Krylov kernels (cooperative launch)
