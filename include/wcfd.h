@@ -68,6 +68,9 @@ typedef struct wcfd_mesh {
     const float*   cell_volume;   /* [C]                                               */
     const int32_t* ell_col;       /* [W*C] slot-major neighbour column; padding = own row */
     const int32_t* boundary_face; /* [B]   face id of each boundary row               */
+    const float*   face_dvec;     /* [K*4] owner->neighbour centroid vector d (internal faces)
+                                     and 0; read only by the opt-in explicit internal terms
+                                     (wcfd_params.explicit_terms), may be NULL otherwise */
 } wcfd_mesh;
 
 /* boundary tables, one row per boundary face, columns u,v,w,p */
@@ -139,6 +142,11 @@ typedef struct wcfd_params {
     double  p_refine_rtol;  /* relative tolerance of each sweep's fp32 CG correction solve */
     double  rtol_u;         /* momentum stop also at ||r|| <= rtol_u ||r_0||; 0 = atol only (the reference) */
     double  rtol_p;         /* pressure stop also at ||r|| <= rtol_p ||r_0||; 0 = atol only (the reference) */
+    int32_t explicit_terms; /* opt-in internal-face explicit weights in the RHS (the reference
+                               drops them): bit0 convection (skew correction), bit1 with
+                               the upwindLinear term, bit2 the non-orthogonal diffusion
+                               part (momentum and pressure); 0 = the reference          */
+    int32_t pad2_;
 } wcfd_params;
 
 /* a full case: everything one SIMPLE iteration touches */

@@ -23,7 +23,8 @@ What it restates, step by step, with the reference file:line of each piece:
 * explicit p relaxation ......... FV/model.py:381-384
 
 including the quirks that change numbers: explicit weights of internal faces never
-reach the RHS (equation_kernels.py:84-101 loops over boundary faces only); a p-only
+reach the RHS (equation_kernels.py:84-101 loops over boundary faces only; the opt-in
+``explicit_internal`` option, not the reference's path, adds them); a p-only
 gradient zeroes every field's gradient (model.py:237); rUA uses the relaxed u-row
 diagonal for all three components (solver_kernels.py:14-16); term scale is assigned,
 not multiplied (terms.py:92-113).
@@ -186,7 +187,7 @@ class OracleCase:
 
     def __init__(self, geo: dict, bc_type, bc_value, viscosity, density, *, T=np.float64, R=np.float64,
                  reference_cell=None, reference_value=0.0, correction=False, skew_correction=True,
-                 atol=None, maxiter=500, rhie_chow=False):
+                 atol=None, maxiter=500, rhie_chow=False, explicit_internal=False, conv_scheme="upwind"):
         self.g = Geometry(geo, T)
         self.T, self.R = T, R
         g = self.g
@@ -198,6 +199,8 @@ class OracleCase:
         self.correction = correction
         self.skew = skew_correction
         self.rhie_chow = rhie_chow
+        self.explicit_internal = explicit_internal
+        self.conv_scheme = conv_scheme
         self.atol = atol if atol is not None else (1e-5 if T == np.float32 else 1e-6)
         self.maxiter = maxiter
         self.cell_values = np.zeros((C, 4), dtype=T)
@@ -324,9 +327,13 @@ class OracleCase:
         return acc
 
     # ---- term weights -----------------------------------------------------------------
-    def convection_weights(self, fields=(0, 1, 2), scheme="upwind"):
-        """convection.py:43-91 -> (C,F,n,3) [owner, neighbour, explicit]."""
+    def convection_weights(self, fields=(0, 1, 2), scheme=None):
+        """convection.py:43-91 -> (C,F,n,3) [owner, neighbour, explicit].  upwindLinear
+        (convectionScheme.py:54-88) adds grad(phi)_up . (r_f - r_up) to the explicit weight,
+        with the upwind cell's own centroid-to-face vector (the reference's neighbour branch
+        reads the owner's, Q12)."""
         g, T = self.g, self.T
+        scheme = self.conv_scheme if scheme is None else scheme
         n = len(fields)
         w = np.zeros((g.C, g.F, n, 3), dtype=T)
         b = g.boundary_ids
@@ -334,7 +341,7 @@ class OracleCase:
             w[g.P[b], g.cell_face_index[b, 0], j, 2] = self.mass_fluxes[b] * self.face_values[b, o]
         ii = g.internal_ids
         m = self.mass_fluxes[ii]
-        if scheme == "upwind":
+        if scheme in ("upwind", "upwindLinear"):
             fw0 = np.where(m > 0, T(1.0), T(0.0)).astype(T)
             fw1 = np.where(m > 0, T(0.0), T(1.0)).astype(T)
         elif scheme == "central difference":
@@ -348,9 +355,13 @@ class OracleCase:
             d = g.face_centroid[ii] - rk_dash
         for j, o in enumerate(fields):
             fw2 = np.zeros_like(m)
-            if self.skew:  # computed as the reference does; never reaches the RHS (Q1)
+            if self.skew:  # computed as the reference does; reaches the RHS only opt-in (Q1)
                 gi = (self.cell_gradients[P, j] * g.psi[ii][:, None] + g.psi2[ii][:, None] * self.cell_gradients[N, j])
                 fw2 = np.sum(gi * d, axis=1, dtype=T)
+            if scheme == "upwindLinear":
+                up = np.where(m > 0, P, N)
+                rvec = (g.face_centroid[ii] - g.centroid[up]).astype(T)
+                fw2 = (fw2 + np.sum(self.cell_gradients[up, j] * rvec, axis=1, dtype=T)).astype(T)
             w[P, sP, j, 0] = fw0 * m
             w[P, sP, j, 1] = fw1 * m
             w[P, sP, j, 2] = fw2 * m
@@ -442,6 +453,13 @@ class OracleCase:
             b = g.boundary_ids
             for o in range(n):
                 np.add.at(rhs[:, o], g.P[b], -s * w[g.P[b], g.cell_face_index[b, 0], o, 2])
+            if self.explicit_internal:
+                # opt-in (not the reference's path, Q1): internal explicit weights reach the
+                # RHS the way the boundary ones do
+                ii = g.internal_ids
+                for o in range(n):
+                    np.add.at(rhs[:, o], g.P[ii], -s * w[g.P[ii], g.cell_face_index[ii, 0], o, 2])
+                    np.add.at(rhs[:, o], g.N[ii], -s * w[g.N[ii], g.cell_face_index[ii, 1], o, 2])
         for w, s in cell_terms:
             s = T(s)
             for o in range(n):

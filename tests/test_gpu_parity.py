@@ -568,3 +568,31 @@ def test_reference_style_loop_matches_fused_step():
         for o in range(3):
             assert vel_err(gb, ga, o) < 1e-5, (it, o)
         assert rel_l2(gb[:, 3], ga[:, 3]) < 1e-4, it
+
+
+@pytest.mark.parametrize("variant", ["skew", "corrected", "upwind_linear"])
+def test_explicit_internal_terms_option_tracks_oracle(variant):
+    """Opt-in internal-face explicit weights (IncompressibleSolver.explicit_internal_terms):
+    the convection skew term, the upwindLinear term and the non-orthogonal diffusion part
+    reach the RHS on the GPU as in the oracle's restatement of the same option."""
+    m = cavity_mesh(16, jitter=0.15, seed=11)
+    corr = variant == "corrected"
+    model, solver, oc = make_pair(m, cavity_bc, correction=corr)
+    solver.explicit_internal_terms = True
+    oc.explicit_internal = True
+    if variant == "upwind_linear":
+        solver.convection.interpolation = "upwindLinear"
+        oc.conv_scheme = "upwindLinear"
+    for it in range(4):
+        solver.step()
+        oracle_step(oc)
+        g = fields(model)
+        tol_u = 1e-5 if it == 0 else 1e-4
+        tol_p = 1e-4 if it == 0 else 1e-3
+        for o in range(3):
+            assert vel_err(g, oc.cell_values, o) < tol_u, (it, o)
+        assert rel_l2(g[:, 3], oc.cell_values[:, 3]) < tol_p, it
+    m2, s2, _ = make_pair(m, cavity_bc, correction=corr)
+    for _ in range(4):
+        s2.step()
+    assert not torch.equal(model.cell_values, m2.cell_values)

@@ -57,6 +57,8 @@ def build_geometry(mesh, correction: bool = False) -> dict:
     face_normal = np.zeros((K, 4), dtype=np.float32)
     face_normal[:, :3] = n_own
     face_normal[:, 3] = area
+    face_dvec = np.zeros((K, 4), dtype=np.float32)
+    face_dvec[:, :3] = dvec
 
     vol = g["volume"]
     faces = cp.faces.astype(np.int64)
@@ -80,5 +82,5 @@ def build_geometry(mesh, correction: bool = False) -> dict:
         face_owner=P.astype(np.int32), face_nbr=N.astype(np.int32), face_brow=brow,
         face_interp=face_interp, face_normal=face_normal, face_gdiff=gdiff.astype(np.float32),
         face_rpf=rpf.astype(np.float32), cell_slot=cell_slot, cell_volume=vol.astype(np.float32),
-        ell_col=ell_col.astype(np.int32), boundary_face=bids.astype(np.int32),
+        ell_col=ell_col.astype(np.int32), boundary_face=bids.astype(np.int32), face_dvec=face_dvec,
     )

@@ -61,6 +61,10 @@ class IncompressibleSolver:
         # opt-in Rhie-Chow convecting flux (the reference re-interpolates the flux from the
         # corrected cell velocities, incompressible.py:97-99)
         self.rhie_chow = False
+        # opt-in: internal-face explicit weights (skew correction of the convection, the
+        # upwindLinear term when convection.interpolation == 'upwindLinear', the
+        # non-orthogonal diffusion part) reach the RHS; the reference drops them
+        self.explicit_internal_terms = False
         self.p_x64 = None
         self.p_work = None
         self._graph = None
@@ -105,7 +109,15 @@ class IncompressibleSolver:
                              int(bool(m.skew_correction)), float(self.vel_equation.tol),
                              float(self.p_corr_equation.tol), int(self.p_refine), int(bool(self.rhie_chow)),
                              float(self.p_refine_rtol),
-                             float(self.vel_equation.rtol), float(self.p_corr_equation.rtol))
+                             float(self.vel_equation.rtol), float(self.p_corr_equation.rtol), self._explicit_bits())
+
+    def _explicit_bits(self) -> int:
+        if not self.explicit_internal_terms:
+            return 0
+        bits = (1 if self.model.skew_correction else 0) | (4 if self.correction else 0)
+        if self.convection.interpolation == "upwindLinear":
+            bits |= 2
+        return bits
 
     def _param_key(self):
         m = self.model
@@ -113,7 +125,8 @@ class IncompressibleSolver:
                 self.p_relaxation_factor, self.dt, m.reference_pressure_cell_id, m.reference_pressure,
                 self.NUM_INNER_LOOPS, self.NUM_ORTHOGONAL_CORRECTORS, self.vel_equation.max_iter,
                 m.skew_correction, self.vel_equation.tol, self.p_corr_equation.tol, self._events_ptr,
-                self.p_refine, self.p_refine_rtol, self.vel_equation.rtol, self.p_corr_equation.rtol, self.rhie_chow)
+                self.p_refine, self.p_refine_rtol, self.vel_equation.rtol, self.p_corr_equation.rtol, self.rhie_chow,
+                self._explicit_bits())
 
     def case_struct(self) -> _lib.Case_t:
         """The C struct of this case; rebuilt only when a parameter changed (the device

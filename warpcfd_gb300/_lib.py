@@ -42,7 +42,7 @@ class Mesh_t(ct.Structure):
                 ("faces_per_cell", ct.c_int32), ("ell_width", ct.c_int32), ("pad_", ct.c_int32),
                 ("face_owner", vp), ("face_nbr", vp), ("face_brow", vp), ("face_interp", vp),
                 ("face_normal", vp), ("face_gdiff", vp), ("face_rpf", vp), ("cell_slot", vp),
-                ("cell_volume", vp), ("ell_col", vp), ("boundary_face", vp)]
+                ("cell_volume", vp), ("ell_col", vp), ("boundary_face", vp), ("face_dvec", vp)]
 
 
 class BC_t(ct.Structure):
@@ -72,7 +72,8 @@ class Params_t(ct.Structure):
                 ("dt", ct.c_float), ("ref_value", ct.c_float), ("ref_cell", ct.c_int32), ("steady", ct.c_int32),
                 ("n_inner", ct.c_int32), ("n_ortho", ct.c_int32), ("maxiter", ct.c_int32), ("skew", ct.c_int32),
                 ("atol_u", ct.c_double), ("atol_p", ct.c_double), ("p_refine", ct.c_int32), ("rhie_chow", ct.c_int32),
-                ("p_refine_rtol", ct.c_double), ("rtol_u", ct.c_double), ("rtol_p", ct.c_double)]
+                ("p_refine_rtol", ct.c_double), ("rtol_u", ct.c_double), ("rtol_p", ct.c_double),
+                ("explicit_terms", ct.c_int32), ("pad2_", ct.c_int32)]
 
 
 class Case_t(ct.Structure):

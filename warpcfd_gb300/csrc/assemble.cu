@@ -22,8 +22,52 @@ namespace wcfd {
 //   implicit relaxation (equation_kernels.py:128-152):
 //     rhs += (1-a)/a diag phi ; diag /= a
 //   rUA = V / (diag_u rho) (solver_kernels.py:6-16)
-// Internal-face explicit weights never reach the RHS (equation_kernels.py:84-101), so
-// none are formed here.
+// Internal-face explicit weights never reach the RHS in the reference
+// (equation_kernels.py:84-101), so by default none are formed here.  Opt-in
+// (prm.explicit_terms, not the reference's path), they enter the RHS as the boundary
+// ones do (b -= scale w2):
+//   convection: w2 = (+mdot owner, -mdot neighbour) E, E the sum of
+//     bit0  grad(phi)_f . skew (convection.py:76-78, skewness_functions.py:6-19) and
+//     bit1  upwindLinear: grad(phi)_up . (r_f - r_up) (convectionScheme.py:54-88, with the
+//           upwind cell's own centroid-to-face vector)
+//   bit2  diffusion, non-orthogonal part: w2 = (+owner, -neighbour) nu A grad(phi)_f . n2,
+//         n2 = n - d / (n . d) (laplacianScheme.py:39-67)
+// with grad(phi)_f = psi grad(phi)_P + (1 - psi) grad(phi)_N; they need face_dvec.
+__device__ __forceinline__ void explicit_internal_terms(const wcfd_mesh& m, const wcfd_state& s, int k, bool owner_side,
+                                                        float md, float nu, int bits, int field0, int nf, float* b,
+                                                        float scale_conv, float scale_diff) {
+    const int P = __ldg(m.face_owner + k), N = __ldg(m.face_nbr + k);
+    const float4 si = __ldg(reinterpret_cast<const float4*>(m.face_interp) + k);
+    const float4 dv = __ldg(reinterpret_cast<const float4*>(m.face_dvec) + k);
+    const float4 nn = __ldg(reinterpret_cast<const float4*>(m.face_normal) + k);
+    const float psi = si.w, psi2 = 1.0f - psi;
+    const float side = owner_side ? 1.0f : -1.0f;
+    const float* gP = s.cell_gradients + 12 * (size_t)P;
+    const float* gN = s.cell_gradients + 12 * (size_t)N;
+    for (int q = 0; q < nf; ++q) {
+        const int o = field0 + q;
+        const float gx = gP[3 * o] * psi + psi2 * gN[3 * o];
+        const float gy = gP[3 * o + 1] * psi + psi2 * gN[3 * o + 1];
+        const float gz = gP[3 * o + 2] * psi + psi2 * gN[3 * o + 2];
+        if (bits & 3) {
+            float e = (bits & 1) ? gx * si.x + gy * si.y + gz * si.z : 0.0f;
+            if (bits & 2) {
+                const bool up_owner = md > 0.0f;
+                const float* gu = up_owner ? gP + 3 * o : gN + 3 * o;
+                const float a = up_owner ? psi2 : -psi;  // r_f - r_up = skew + a d
+                e += gu[0] * (si.x + a * dv.x) + gu[1] * (si.y + a * dv.y) + gu[2] * (si.z + a * dv.z);
+            }
+            b[q] -= scale_conv * (side * md * e);
+        }
+        if (bits & 4) {
+            const float nd = nn.x * dv.x + nn.y * dv.y + nn.z * dv.z;
+            const float inv = 1.0f / nd;
+            const float n2x = nn.x - dv.x * inv, n2y = nn.y - dv.y * inv, n2z = nn.z - dv.z * inv;
+            b[q] -= scale_diff * (side * nu * nn.w * (gx * n2x + gy * n2y + gz * n2z));
+        }
+    }
+}
+
 __device__ __forceinline__ void momentum_assemble_body(const wcfd_mesh& m, const wcfd_bc& bc, const wcfd_state& s, const wcfd_system& sys, float* __restrict__ rua, const wcfd_params& prm, int c) {
     const int C = m.n_cells;
     const float nu = prm.nu;
@@ -52,6 +96,7 @@ __device__ __forceinline__ void momentum_assemble_body(const wcfd_mesh& m, const
             dsum += w0 + dcoef;
             sys.off[(size_t)j * C + c] = w1 - dcoef;
             ++j;
+            if (prm.explicit_terms) explicit_internal_terms(m, s, k, owner_side, md, nu, prm.explicit_terms, 0, 3, b, 1.0f, -1.0f);
         } else {
             const int br = __ldg(m.face_brow + k);
             const uchar4 t = __ldg(reinterpret_cast<const uchar4*>(bc.type) + br);
@@ -154,6 +199,8 @@ __device__ __forceinline__ void pressure_assemble_body(const wcfd_mesh& m, const
             d -= coef;
             sys.off[(size_t)j * C + c] = ref ? 0.0f : coef;
             ++j;
+            if (prm.explicit_terms & 4)  // opt-in non-orthogonal explicit part (see momentum)
+                explicit_internal_terms(m, s, k, sk >= 0, 0.0f, rua_faces[k], 4, 3, 1, &b, 0.0f, 1.0f);
         } else {
             const int br = __ldg(m.face_brow + k);
             const uint8_t t = __ldg(bc.type + 4 * (size_t)br + 3);
