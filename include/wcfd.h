@@ -64,7 +64,9 @@ typedef struct wcfd_mesh {
     const float*   face_gdiff;    /* [K]   area/|d| (internal; x|n1| when corrected), area/|r_Pf| (boundary) */
     const float*   face_rpf;      /* [K]   |r_P->f| (owner centroid to face centroid) */
     const float*   cell_slot;     /* [F*C*4] slot-major: A n_cf / V (3), bits of the signed face id
-                                     (k for the owner side, ~k for the neighbour side) */
+                                     (k for the owner side, ~k for the neighbour side;
+                                     INT32_MIN with a zero vector: a null slot of a cell
+                                     with fewer faces than F in a mixed mesh) */
     const float*   cell_volume;   /* [C]                                               */
     const int32_t* ell_col;       /* [W*C] slot-major neighbour column; padding = own row */
     const int32_t* boundary_face; /* [B]   face id of each boundary row               */

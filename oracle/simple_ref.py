@@ -60,12 +60,12 @@ def geometry_from_mesh(mesh) -> dict:
         to_face=g["to_face"], centroid=g["centroid"], volume=g["volume"],
         adjacent=adj, cell_face_index=cfi, is_boundary=fp.is_boundary.astype(np.int64),
         face_centroid=g["face_centroid"],
-        distance=np.where(fp.is_boundary[:, None] == 0,
-                          g["centroid"][np.maximum(adj[:, 1], 0)] - g["centroid"][adj[:, 0]], -1.0),
+        distance=fp.distance.astype(np.float64),   # float32 centroid difference (mesh.py:276)
         internal_ids=fp.internal_face_ids.astype(np.int64),
         boundary_ids=fp.boundary_face_ids.astype(np.int64),
         nnz_per_cell=cp.nnz_per_cell.astype(np.int64),
         face_offset_index=cp.face_offset_index.astype(np.int64),
+        slot_valid=(cp.faces >= 0),
     )
 
 
@@ -280,9 +280,10 @@ class OracleCase:
         """model.py:232-239: zero every field's gradient, then Green-Gauss for ``out``."""
         g = self.g
         self.cell_gradients[...] = 0
-        area = g.area[g.cell_faces]                                  # (C,F)
+        # null slots of mixed meshes (face id -1) have zero normals; mask them anyway
+        area = np.where(g.slot_valid, g.area[g.cell_faces], 0).astype(self.T)   # (C,F)
         for o in out:
-            phi = self.face_values[g.cell_faces, o]                  # (C,F)
+            phi = np.where(g.slot_valid, self.face_values[g.cell_faces, o], 0).astype(self.T)  # (C,F)
             vec = (phi * area)[..., None] * g.normal / g.volume[:, None, None]
             acc = np.zeros((g.C, 3), dtype=self.T)
             for f in range(g.F):
@@ -319,7 +320,7 @@ class OracleCase:
     def div_flux(self):
         """model_kernels.py:26-34."""
         g = self.g
-        m = self.mass_fluxes[g.cell_faces]
+        m = np.where(g.slot_valid, self.mass_fluxes[g.cell_faces], 0).astype(self.T)
         sgn = np.where(g.face_side == 0, m, -m)
         acc = np.zeros(g.C, dtype=self.T)
         for f in range(g.F):

@@ -51,6 +51,26 @@ def cavity3d_bc(b, lid=1.0):
     b.velocity_BC("+Y", u=lid, v=0, w=0)
 
 
+def prism_cavity_mesh(n=16, element_type="mixed", jitter=0.0, seed=0):
+    """The 2D cavity with prisms: 'wedge' cuts every quad, 'mixed' the right half."""
+    m = Mesh(create_2D_grid((0, 0, 0), n, n, 1.0, 1.0, 0.1, element_type=element_type, jitter=jitter, seed=seed))
+    define_boundary_walls(m)
+    return m
+
+
+def prism_channel_mesh(nx=40, ny=8, lx=10.0, ly=1.0, element_type="wedge"):
+    m = Mesh(create_2D_grid((0, 0, 0), nx, ny, lx, ly, 0.1, element_type=element_type))
+    define_boundary_walls(m)
+    return m
+
+
+def mixed_cavity3d_mesh(n=6, prism_fraction=0.5, seed=0):
+    """The 3D cavity with a seeded fraction of its hexes cut into two prisms each."""
+    m = Mesh(create_3D_grid((0, 0, 0), n, n, n, 1.0, 1.0, 1.0, prism_fraction=prism_fraction, seed=seed))
+    define_boundary_walls(m)
+    return m
+
+
 def host_boundary(m, bc_fn, **kw):
     b = Boundary(FIELDS, m.groups, m.face_properties.boundary_face_ids)
     bc_fn(b, **kw)

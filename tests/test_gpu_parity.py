@@ -13,7 +13,8 @@ import numpy as np
 import pytest
 import torch
 
-from tests.cases import cavity3d_bc, cavity3d_mesh, cavity_bc, cavity_mesh, channel_bc, channel_mesh
+from tests.cases import (cavity3d_bc, cavity3d_mesh, cavity_bc, cavity_mesh, channel_bc, channel_mesh,
+                         mixed_cavity3d_mesh, prism_cavity_mesh, prism_channel_mesh)
 from tests.gpu_helpers import fields, make_pair, oracle_step, rel_l2, vel_err
 
 pytestmark = pytest.mark.gpu
@@ -83,11 +84,13 @@ def test_upwind_face_interpolation():
     np.testing.assert_allclose(fv[ii], oc.cell_values[up] + skew, rtol=1e-5, atol=1e-6)
 
 
-@pytest.mark.parametrize("case", ["cavity", "channel", "cavity3d"])
+@pytest.mark.parametrize("case", ["cavity", "channel", "cavity3d", "prism_channel", "mixed_cavity3d"])
 def test_assembly_matches_oracle(case):
     mk = {"cavity": (lambda: cavity_mesh(10, jitter=0.1, seed=1), cavity_bc, 0),
           "channel": (lambda: channel_mesh(20, 5), channel_bc, None),
-          "cavity3d": (lambda: cavity3d_mesh(5), cavity3d_bc, 0)}[case]
+          "cavity3d": (lambda: cavity3d_mesh(5), cavity3d_bc, 0),
+          "prism_channel": (lambda: prism_channel_mesh(20, 5), channel_bc, None),
+          "mixed_cavity3d": (lambda: mixed_cavity3d_mesh(5, 0.5, seed=1), cavity3d_bc, 0)}[case]
     m = mk[0]()
     model, solver, oc = make_pair(m, mk[1], ref_cell=mk[2])
     _seed_state(model, oc, 4)
@@ -596,3 +599,28 @@ def test_explicit_internal_terms_option_tracks_oracle(variant):
     for _ in range(4):
         s2.step()
     assert not torch.equal(model.cell_values, m2.cell_values)
+
+
+@pytest.mark.parametrize("case", ["prism_cavity", "mixed_cavity_skew", "prism_channel", "mixed_cavity3d"])
+def test_prism_and_mixed_meshes_track_oracle(case):
+    """Wedge meshes and mixed hex/prism meshes (null slots past a wedge's five faces):
+    the GPU step follows the oracle on the same mesh, corrected and uncorrected.  The
+    prism channel is 5 long: on a 10-long one the oracle's own results move by 1.1e-5
+    when only the summation order of its SpMV changes, above the 1e-5 bound."""
+    mk = {"prism_cavity": (lambda: prism_cavity_mesh(12, "wedge"), cavity_bc, 0, 0.01, False),
+          "mixed_cavity_skew": (lambda: prism_cavity_mesh(16, "mixed", jitter=0.1, seed=5), cavity_bc, 0, 0.01, True),
+          "prism_channel": (lambda: prism_channel_mesh(20, 5, lx=5.0), channel_bc, None, 0.05, False),
+          "mixed_cavity3d": (lambda: mixed_cavity3d_mesh(8, 0.5, seed=2), cavity3d_bc, 0, 0.01, True)}[case]
+    m = mk[0]()
+    model, solver, oc = make_pair(m, mk[1], ref_cell=mk[2], nu=mk[3], correction=mk[4])
+    for it in range(5):
+        solver.step()
+        oracle_step(oc)
+        g = fields(model)
+        tol_u = 1e-5 if it == 0 else 1e-4
+        tol_p = 1e-4 if it == 0 else 1e-3
+        for o in range(3):
+            assert vel_err(g, oc.cell_values, o) < tol_u, (it, o)
+        assert rel_l2(g[:, 3], oc.cell_values[:, 3]) < tol_p, it
+        st = solver.solve_stats()
+        assert abs(st[1]["iterations"] - oc.log[-1][2]) <= 2

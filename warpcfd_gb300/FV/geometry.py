@@ -1,8 +1,15 @@
 """Device geometry: the SoA arrays the kernels read, derived once per mesh on the host.
 
-All derived quantities are computed in float64 from the mesh pass and rounded once to
-float32.  Their definitions follow the reference's struct initialisation
-(warp_cfd/FV/mesh_structs.py:141-251) and term kernels:
+Quantities the reference derives in float32 from its float32 mesh arrays are derived
+the same way here, in float32 and in the same order of operations: the centroid
+distance d (mesh.py:276), psi (mesh_structs.py:206-209), the skew vector
+(skewness_functions.py:15-16, evaluated there per use from the same float32 operands),
+|r_P->f| and the diffusion coefficients.  On meshes whose centroids are not exact in
+float32 (prisms, jittered nodes, domains far from the origin) the differences of nearby
+centroids cancel digits, and deriving these in float64 instead would move the results
+away from the reference's by more than its own rounding.  The Green-Gauss slot vectors
+are rounded once from float64.  Definitions (warp_cfd/FV/mesh_structs.py:141-251 and the
+term kernels):
 
 * psi = |r_P->f| / |r_P - r_N| (mesh_structs.py:206-209); 0 on boundary faces;
 * skew = r_f - (psi r_P + (1 - psi) r_N) (skewness_functions.py:6-19);
@@ -10,7 +17,9 @@ float32.  Their definitions follow the reference's struct initialisation
 * gdiff = A/|d| on internal faces (laplacianScheme.py:14-34), A |n1|/|d| with the
   non-orthogonal correction (laplacianScheme.py:39-67, n1 = d/(n_f . d)), and A/|r_Pf|
   on boundary faces (diffusion.py:145-146);
-* cell slot vector = n_cf A_f / V_c, the Green-Gauss weight (model_kernels.py:83-88).
+* cell slot vector = n_cf A_f / V_c, the Green-Gauss weight (model_kernels.py:83-88);
+* a null slot (a cell of a mixed mesh with fewer faces than F) holds NULL_SLOT as its
+  face reference and a zero vector; the kernels skip it.
 
 Layout (HBM): per-face arrays are indexed by the reference's face id; per-cell slot data
 and the off-diagonal pattern are slot-major ([F][C], [W][C]) so a warp of consecutive
@@ -21,29 +30,34 @@ from __future__ import annotations
 import numpy as np
 
 
+NULL_SLOT = np.int32(-2**31)  # the face reference of a null slot (kNullSlot in the kernels)
+
+
 def build_geometry(mesh, correction: bool = False) -> dict:
     fp, cp, g = mesh.face_properties, mesh.cell_properties, mesh._geometry64
+    f4 = np.float32
     C, F = cp.faces.shape
     K = fp.unique_faces.shape[0]
     P = fp.adjacent_cells[:, 0].astype(np.int64)
     N = fp.adjacent_cells[:, 1].astype(np.int64)
     sP = fp.cell_face_index[:, 0].astype(np.int64)
-    cent = g["centroid"]
-    area = g["area"][P, sP]
-    n_own = g["normal"][P, sP]
-    rpf = np.linalg.norm(g["to_face"][P, sP], axis=1)
+    cent = g["centroid"].astype(f4)
+    area = g["area"][P, sP].astype(f4)
+    n_own = g["normal"][P, sP].astype(f4)
+    rpf = np.linalg.norm(g["to_face"][P, sP].astype(f4), axis=1)
     internal = N >= 0
     ii = np.nonzero(internal)[0]
-    dvec = np.zeros((K, 3))
-    dvec[ii] = cent[N[ii]] - cent[P[ii]]
+    dvec = np.zeros((K, 3), dtype=f4)
+    dvec[ii] = fp.distance[ii].astype(f4)
     dmag = np.linalg.norm(dvec, axis=1)
-    psi = np.zeros(K)
-    psi[ii] = rpf[ii] / dmag[ii]
-    skew = np.zeros((K, 3))
-    skew[ii] = g["face_centroid"][ii] - (psi[ii, None] * cent[P[ii]] + (1.0 - psi[ii, None]) * cent[N[ii]])
+    psi = np.zeros(K, dtype=f4)
+    psi[ii] = rpf[ii] / np.linalg.norm(cent[P[ii]] - cent[N[ii]], axis=1)
+    psi2 = (f4(1.0) - psi).astype(f4)
+    skew = np.zeros((K, 3), dtype=f4)
+    skew[ii] = g["face_centroid"][ii].astype(f4) - (cent[P[ii]] * psi[ii, None] + cent[N[ii]] * psi2[ii, None])
     gdiff = area / rpf                                   # boundary value; internal overwritten
     if correction:
-        n1 = dvec[ii] / np.sum(n_own[ii] * dvec[ii], axis=1)[:, None]
+        n1 = dvec[ii] * (f4(1.0) / np.sum(n_own[ii] * dvec[ii], axis=1, dtype=f4))[:, None]
         gdiff[ii] = area[ii] * np.linalg.norm(n1, axis=1) / dmag[ii]
     else:
         gdiff[ii] = area[ii] / dmag[ii]
@@ -63,8 +77,13 @@ def build_geometry(mesh, correction: bool = False) -> dict:
     vol = g["volume"]
     faces = cp.faces.astype(np.int64)
     side = cp.face_side.astype(np.int64)
-    svec = g["normal"] * area[faces][..., None] / vol[:, None, None]   # (C,F,3)
+    real = faces >= 0
+    area64 = g["area"][P, sP]
+    svec = g["normal"] * area64[np.maximum(faces, 0)][..., None] / vol[:, None, None]   # (C,F,3)
     signed = np.where(side == 0, faces, ~faces).astype(np.int32)
+    if not real.all():
+        svec[~real] = 0.0
+        signed[~real] = NULL_SLOT
     cell_slot = np.zeros((F, C, 4), dtype=np.float32)
     cell_slot[..., :3] = svec.transpose(1, 0, 2)
     cell_slot[..., 3] = np.ascontiguousarray(signed.T).view(np.float32)

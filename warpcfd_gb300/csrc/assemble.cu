@@ -78,6 +78,7 @@ __device__ __forceinline__ void momentum_assemble_body(const wcfd_mesh& m, const
     const float4* slots = reinterpret_cast<const float4*>(m.cell_slot);
     for (int f = 0; f < m.faces_per_cell; ++f) {
         const int sk = __float_as_int(__ldg(&slots[(size_t)f * C + c].w));
+        if (sk == kNullSlot) continue;
         const bool owner_side = sk >= 0;
         const int k = owner_side ? sk : ~sk;
         const float md = s.mass_fluxes[k];
@@ -192,6 +193,7 @@ __device__ __forceinline__ void pressure_assemble_body(const wcfd_mesh& m, const
     const float4* slots = reinterpret_cast<const float4*>(m.cell_slot);
     for (int f = 0; f < m.faces_per_cell; ++f) {
         const int sk = __float_as_int(__ldg(&slots[(size_t)f * C + c].w));
+        if (sk == kNullSlot) continue;
         const int k = sk >= 0 ? sk : ~sk;
         const int N = __ldg(m.face_nbr + k);
         const float coef = rua_faces[k] * __ldg(m.face_gdiff + k);

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <climits>
 
 #include "wcfd.h"
 
@@ -13,6 +14,9 @@ constexpr int kBlock = 256;      // threads of the one-thread-per-face/cell kern
 constexpr int kMaxFieldBlock = 512;  // largest block of the batched field kernels (a launch parameter)
 constexpr int kSolverBlock = 512;  // threads of the persistent Krylov kernels
 constexpr int kMaxSlots = 6;     // faces per cell (hex)
+// face reference of a null slot: a cell of a mixed mesh with fewer faces than the
+// mesh's faces_per_cell (a wedge or a tetrahedron among hexes); its weights are zero
+constexpr int kNullSlot = INT_MIN;
 constexpr int kClusterBlock = 1024;  // threads per CTA of the cluster-resident solver
 
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }

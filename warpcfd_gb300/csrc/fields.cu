@@ -128,6 +128,7 @@ __device__ __forceinline__ void gradient_body(const wcfd_mesh& m, const wcfd_sta
     for (int f = 0; f < m.faces_per_cell; ++f) {
         const float4 sl = __ldg(slots + (size_t)f * C + c);
         const int sk = __float_as_int(sl.w);
+        if (sk == kNullSlot) continue;
         const int k = sk >= 0 ? sk : ~sk;
         const float4 fv = ld4(s.face_values + 4 * (size_t)k);
 #pragma unroll
@@ -187,6 +188,7 @@ __device__ __forceinline__ void div_body(const wcfd_mesh& m, const float* __rest
     float dv = 0.0f;
     for (int f = 0; f < m.faces_per_cell; ++f) {
         const int sk = __float_as_int(__ldg(&slots[(size_t)f * C + c].w));
+        if (sk == kNullSlot) continue;
         const float md = mdot[sk >= 0 ? sk : ~sk];
         dv += sk >= 0 ? md : -md;
     }

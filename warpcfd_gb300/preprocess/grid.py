@@ -14,7 +14,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .mesh import HEXAHEDRON, Mesh, UnstructuredGrid
+from .mesh import HEXAHEDRON, WEDGE, Mesh, UnstructuredGrid
 
 
 def _hex_connectivity(nx, ny, nz):
@@ -31,6 +31,34 @@ def _hex_connectivity(nx, ny, nz):
     conn = np.stack([n0, n0 + 1, n0 + 1 + sx, n0 + sx,
                      n0 + sy, n0 + 1 + sy, n0 + 1 + sx + sy, n0 + sx + sy], axis=1)
     return conn.astype(np.int64)
+
+
+def _cells_with_prisms(conn, split):
+    """VTK cells of a hex lattice in which the hexes where ``split`` is True are cut into
+    two wedges along the diagonal (node 0 -> node 2) of their bottom quad.  A wedge keeps
+    VTK's order (triangle 0-1-2 counter-clockwise seen from its opposite triangle 3-4-5),
+    so the wedge face table yields outward normals.  Cells stay in lattice order, the two
+    wedges of a hex one after the other."""
+    C = conn.shape[0]
+    split = np.asarray(split, dtype=bool)
+    n_out = C + int(split.sum())
+    first = np.arange(C) + np.concatenate([[0], np.cumsum(split)[:-1]])  # output id of each hex's first cell
+    types = np.full(n_out, HEXAHEDRON, dtype=np.int64)
+    types[first[split]] = WEDGE
+    types[first[split] + 1] = WEDGE
+    npc = np.where(types == HEXAHEDRON, 8, 6)
+    flat = np.empty(int((npc + 1).sum()), dtype=np.int64)
+    start = np.concatenate([[0], np.cumsum(npc + 1)[:-1]])
+    flat[start] = npc
+    h = ~split
+    for j in range(8):
+        flat[start[first[h]] + 1 + j] = conn[h, j]
+    a = conn[split][:, [0, 1, 2, 4, 5, 6]]
+    b = conn[split][:, [0, 2, 3, 4, 6, 7]]
+    for j in range(6):
+        flat[start[first[split]] + 1 + j] = a[:, j]
+        flat[start[first[split] + 1] + 1 + j] = b[:, j]
+    return flat, types
 
 
 def _lattice(origin, nx, ny, nz, lx, ly, lz):
@@ -72,26 +100,44 @@ def create_2D_grid(origin, nx, ny, dx, dy, dz=0.1, *, element_type="hex", unstru
                    display_mesh=False, save=None, gmsh_version2=False, jitter=0.0, seed=0) -> UnstructuredGrid:
     """Rectangle ``dx`` x ``dy`` at ``origin`` with ``nx`` x ``ny`` hexes, one cell (``dz``) thick.
 
-    Same call shape as warp_cfd/preprocess/grid.py:8.  Only ``element_type='hex'`` is
-    produced (the only cell type that reaches the reference solver).  ``jitter`` > 0
-    moves interior nodes by up to that fraction of the local edge length (seeded).
+    Same call shape as warp_cfd/preprocess/grid.py:8.  ``element_type`` 'hex' (the only
+    cell type the reference's examples run), 'wedge' (every quad cut into two
+    triangles, extruded: a prism mesh) or 'mixed' (the quads of the right half cut, a
+    hex/prism mesh).  ``jitter`` > 0 moves interior nodes by up to that fraction of the
+    local edge length (seeded).
     """
-    if element_type != "hex":
-        raise NotImplementedError("create_2D_grid builds hex meshes only")
+    if element_type not in ("hex", "wedge", "mixed"):
+        raise NotImplementedError("create_2D_grid builds hex, wedge and mixed hex/wedge meshes")
     pts = _lattice(origin, nx, ny, 1, dx, dy, dz)
     if jitter > 0.0:
         pts = jitter_interior_nodes(pts, nx, ny, 1, (dx / nx, dy / ny, dz), jitter, seed, planar_z=True)
     conn = _hex_connectivity(nx, ny, 1)
-    cells = np.hstack([np.full((conn.shape[0], 1), 8), conn]).ravel()
-    return UnstructuredGrid(cells, np.full(conn.shape[0], HEXAHEDRON), pts)
+    if element_type == "hex":
+        cells = np.hstack([np.full((conn.shape[0], 1), 8), conn]).ravel()
+        return UnstructuredGrid(cells, np.full(conn.shape[0], HEXAHEDRON), pts)
+    i = np.arange(conn.shape[0]) % nx
+    split = np.ones(conn.shape[0], dtype=bool) if element_type == "wedge" else i >= nx // 2
+    cells, types = _cells_with_prisms(conn, split)
+    return UnstructuredGrid(cells, types, pts)
 
 
-def create_3D_grid(origin, nx, ny, nz, lx, ly, lz, *, jitter=0.0, seed=0) -> UnstructuredGrid:
-    """Box ``lx`` x ``ly`` x ``lz`` of ``nx`` x ``ny`` x ``nz`` hexes (the 3D cavity case)."""
+def create_3D_grid(origin, nx, ny, nz, lx, ly, lz, *, jitter=0.0, seed=0,
+                   prism_fraction=0.0) -> UnstructuredGrid:
+    """Box ``lx`` x ``ly`` x ``lz`` of ``nx`` x ``ny`` x ``nz`` hexes (the 3D cavity case).
+
+    ``prism_fraction`` > 0 cuts that fraction of the hexes (a seeded random choice) into
+    two wedges each: a mixed hex/prism mesh.  With ``jitter`` the cut hexes' faces are no
+    longer planar, so jitter and prisms are not combined."""
+    if prism_fraction > 0.0 and jitter > 0.0:
+        raise ValueError("prism_fraction needs planar hex faces: use jitter = 0")
     pts = _lattice(origin, nx, ny, nz, lx, ly, lz)
     if jitter > 0.0:
         pts = jitter_interior_nodes(pts, nx, ny, nz, (lx / nx, ly / ny, lz / nz), jitter, seed)
     conn = _hex_connectivity(nx, ny, nz)
+    if prism_fraction > 0.0:
+        split = np.random.default_rng(seed).random(conn.shape[0]) < prism_fraction
+        cells, types = _cells_with_prisms(conn, split)
+        return UnstructuredGrid(cells, types, pts)
     cells = np.hstack([np.full((conn.shape[0], 1), 8), conn]).ravel()
     return UnstructuredGrid(cells, np.full(conn.shape[0], HEXAHEDRON), pts)
 

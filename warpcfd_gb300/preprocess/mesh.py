@@ -16,6 +16,14 @@ the finite-volume step consumes, with the same meaning and the same numbering as
 Unlike the reference it needs neither pyvista nor gmsh, and the owner/neighbour pass
 is vectorised (the reference walks the neighbour pairs in a Python loop,
 mesh.py:263-281), so a 2.1M-cell hex mesh preprocesses in seconds.
+
+Mixed meshes (hexahedra, wedges and tetrahedra in one grid; the reference accepts one
+cell type, mesh.py:20) are an extension.  Cells keep the grid's order; every cell has
+F = the largest face count of the types present slots, its own faces first in its
+type's table order and then null slots (face id -1, zero area and normal, neighbour -1,
+``slot_valid`` False).  Faces are numbered triangles first, then quadrilaterals, each
+set in lexicographic order of its sorted node ids -- for a single-type mesh exactly the
+reference's numbering (a wedge mesh's triangle set precedes its quad set there too).
 """
 from __future__ import annotations
 
@@ -47,6 +55,33 @@ WEDGE_QUAD_FACES = np.array([[0, 3, 5, 2], [1, 2, 5, 4], [0, 1, 4, 3]], dtype=np
 
 NODES_PER_CELL = {TETRA: 4, HEXAHEDRON: 8, WEDGE: 6}
 
+# per cell type: its local faces in slot order
+CELL_FACES = {HEXAHEDRON: [tuple(f) for f in HEX_FACES],
+              TETRA: [tuple(f) for f in TET_FACES],
+              WEDGE: [tuple(f) for f in WEDGE_TRI_FACES] + [tuple(f) for f in WEDGE_QUAD_FACES]}
+
+
+def padded_connectivity(grid):
+    """(C, 8) int64 node ids in the grid's cell order, -1 past each cell's node count,
+    and the (C,) VTK type of every cell.  Reads ``celltypes`` and the flat VTK ``cells``
+    array ([n, i0 .. i(n-1), n, ...]) of a pyvista-style grid."""
+    types = np.asarray(grid.celltypes, dtype=np.int64).ravel()
+    flat = np.asarray(grid.cells, dtype=np.int64).ravel()
+    C = types.shape[0]
+    npc = np.zeros(C, dtype=np.int64)
+    for t, n in NODES_PER_CELL.items():
+        npc[types == t] = n
+    if np.any(npc == 0):
+        raise AssertionError("only Tetra and Hexahedron and Wedge elements are supported")
+    start = np.concatenate([[0], np.cumsum(npc + 1)[:-1]]) + 1
+    if flat.shape[0] != int((npc + 1).sum()) or np.any(flat[start - 1] != npc):
+        raise ValueError("inconsistent node counts in cell connectivity")
+    conn = -np.ones((C, 8), dtype=np.int64)
+    for j in range(8):
+        has = npc > j
+        conn[has, j] = flat[start[has] + j]
+    return conn, types
+
 
 class UnstructuredGrid:
     """Minimal stand-in for ``pyvista.UnstructuredGrid`` (cells, celltypes, points).
@@ -59,6 +94,7 @@ class UnstructuredGrid:
     def __init__(self, cells, celltypes, points):
         cells = np.asarray(cells, dtype=np.int64).ravel()
         celltypes = np.asarray(celltypes, dtype=np.int64).ravel()
+        self.cells = cells
         self.points = np.asarray(points, dtype=np.float64).reshape(-1, 3)
         self.celltypes = celltypes
         types = np.unique(celltypes)
@@ -169,14 +205,14 @@ class Mesh:
     """Mesh preprocessing with the API of ``warp_cfd.preprocess.Mesh`` (mesh.py:17-302).
 
     ``grid`` is anything with ``.points`` (N,3) and ``.cells_dict`` {vtk type: (C,n)}:
-    a pyvista grid, or :class:`UnstructuredGrid`.  One cell type per mesh, as in the
-    reference (mesh.py:20).
+    a pyvista grid, or :class:`UnstructuredGrid`.  A grid of one cell type is handled as
+    the reference handles it (mesh.py:17-43); a grid that mixes types also needs the
+    flat ``cells`` and ``celltypes`` arrays, and then ``cells`` is (C, 8) padded with -1,
+    ``cell_types`` the VTK type per cell and ``cellType`` ('MIXED', 0).
     """
 
     def __init__(self, grid, dtype=np.float32) -> None:
         cells_dict = grid.cells_dict
-        if len(list(cells_dict.keys())) != 1:
-            raise AssertionError("Meshes can only contain a single cell type for now, Got multiple")
         self.float_dtype = np.float32
         self.int_dtype = np.int32
         self.dtype = dtype
@@ -184,14 +220,27 @@ class Mesh:
         points = np.asarray(grid.points, dtype=np.float64)
         self._nodes64 = points
         self.nodes = points.astype(self.float_dtype)
-        celltype = int(list(cells_dict.keys())[0])
-        if celltype not in (HEXAHEDRON, TETRA, WEDGE):
+        types = [int(t) for t in cells_dict.keys()]
+        if any(t not in (HEXAHEDRON, TETRA, WEDGE) for t in types):
             raise AssertionError("only Tetra and Hexahedron and Wedge elements are supported")
-        self.cellType = (CELL_TYPE_NAMES[celltype], celltype)
-        self.cells = np.asarray(cells_dict[celltype], dtype=self.int_dtype)
-        cells64 = self.cells.astype(np.int64)
-        # VTK's cell centre of a linear cell is its parametric centre = node mean
-        self._centroids64 = points[cells64].mean(axis=1)
+        if len(types) == 1:
+            celltype = types[0]
+            self.cellType = (CELL_TYPE_NAMES[celltype], celltype)
+            self.cells = np.asarray(cells_dict[celltype], dtype=self.int_dtype)
+            self.cell_types = np.full(self.cells.shape[0], celltype, dtype=np.int32)
+            cells64 = self.cells.astype(np.int64)
+            # VTK's cell centre of a linear cell is its parametric centre = node mean
+            self._centroids64 = points[cells64].mean(axis=1)
+        else:
+            if not (hasattr(grid, "cells") and hasattr(grid, "celltypes")):
+                raise AssertionError("a mixed-type grid needs its flat cells and celltypes arrays")
+            conn, ctypes = padded_connectivity(grid)
+            self.cellType = ("MIXED", 0)
+            self.cells = conn.astype(self.int_dtype)
+            self.cell_types = ctypes.astype(np.int32)
+            real = conn >= 0
+            pts = points[np.maximum(conn, 0)] * real[..., None]
+            self._centroids64 = pts.sum(axis=1) / real.sum(axis=1)[:, None]
         self.cell_centroids = self._centroids64.astype(self.float_dtype)
         self.groups: dict[str, group] = {}
         self.gridType = "Unstructured"
@@ -228,40 +277,78 @@ class Mesh:
             self.add_group(name, id, group_type)
 
     # ------------------------------------------------------------------ faces
-    def _face_sets(self):
-        t = self.cellType[1]
-        if t == HEXAHEDRON:
-            return [HEX_FACES]
-        if t == TETRA:
-            return [TET_FACES]
-        return [WEDGE_TRI_FACES, WEDGE_QUAD_FACES]
+    def _face_groups(self, npf):
+        """[(cell ids, slots, (Ct, Fs, npf) local node ids)] of every cell type's faces
+        with ``npf`` nodes, in the type order of the first appearance in the grid."""
+        groups = []
+        types = self.cell_types
+        uniq, first = np.unique(types, return_index=True)
+        for t in uniq[np.argsort(first)]:
+            faces = CELL_FACES[int(t)]
+            slots = [j for j, f in enumerate(faces) if len(f) == npf]
+            if not slots:
+                continue
+            ids = np.nonzero(types == t)[0] if len(uniq) > 1 else np.arange(types.shape[0])
+            table = np.array([faces[j] for j in slots], dtype=np.int64)
+            groups.append((ids, np.array(slots, dtype=np.int64), table))
+        return groups
+
+    @property
+    def faces_per_cell(self):
+        return max(len(CELL_FACES[int(t)]) for t in np.unique(self.cell_types))
 
     def get_faces(self):
-        """Unique faces and per-(cell,slot) face ids, areas, normals (mesh.py:64-159)."""
+        """Unique faces and per-(cell,slot) face ids, areas, normals (mesh.py:64-159).
+
+        Triangles are numbered before quadrilaterals; null slots (cells with fewer faces
+        than F) get face id -1 and zero geometry."""
         cells = self.cells.astype(np.int64)
         C = cells.shape[0]
-        sets = self._face_sets()
-        N = max(s.shape[-1] for s in sets)
+        F = self.faces_per_cell
+        sets = [(npf, self._face_groups(npf)) for npf in (3, 4)]
+        sets = [(npf, g) for npf, g in sets if g]
+        N = max(npf for npf, _ in sets)
+        cell_face_ids = -np.ones((C, F), dtype=np.int64)
+        area = np.zeros((C, F), dtype=np.float64)
+        normal = np.zeros((C, F, 3), dtype=np.float64)
+        to_face = np.zeros((C, F, 3), dtype=np.float64)
         shift = 0
         parts = []
-        for face_idx in sets:
-            faces = cells[:, face_idx]  # (C,Fs,n)
-            fsorted = np.sort(faces, axis=2).reshape(-1, face_idx.shape[-1])
+        single = len(np.unique(self.cell_types)) == 1
+        for npf, groups in sets:
+            rows, row_cell, row_slot = [], [], []
+            for ids, slots, table in groups:
+                # a type's faces of one node count occupy consecutive slots
+                sl = slice(int(slots[0]), int(slots[-1]) + 1)
+                faces = cells[ids][:, table] if not single else cells[:, table]  # (Ct,Fs,npf)
+                a, n = _face_normal_and_area(faces, self._nodes64)
+                if single:
+                    area[:, sl], normal[:, sl] = a, n
+                else:
+                    area[ids, sl], normal[ids, sl] = a, n
+                rows.append(faces.reshape(-1, npf))
+                row_cell.append(np.repeat(ids, len(slots)))
+                row_slot.append(np.tile(slots, len(ids)))
+            faces = rows[0] if len(rows) == 1 else np.concatenate(rows, axis=0)
+            fsorted = np.sort(faces, axis=1)
             unique, inv = _unique_rows(fsorted)
-            cell_face_ids = inv.reshape(C, face_idx.shape[0])
-            area, normal = _face_normal_and_area(faces, self._nodes64)
             fcent = self._nodes64[unique].mean(axis=1)
-            npf = unique.shape[-1]
+            if single:
+                sl = slice(int(groups[0][1][0]), int(groups[0][1][-1]) + 1)
+                ids2 = inv.reshape(C, -1)
+                cell_face_ids[:, sl] = ids2 + shift
+                to_face[:, sl] = fcent[ids2] - self._centroids64[:, None, :]
+            else:
+                rc, rs = np.concatenate(row_cell), np.concatenate(row_slot)
+                cell_face_ids[rc, rs] = inv + shift
+                to_face[rc, rs] = fcent[inv] - self._centroids64[rc]
             if N - npf > 0:
                 unique = np.hstack([unique, -np.ones((unique.shape[0], N - npf), dtype=unique.dtype)])
-            to_face = fcent[cell_face_ids] - self._centroids64[:, None, :]
-            parts.append((unique, cell_face_ids + shift, area, normal,
-                          np.full(len(unique), npf, dtype=np.int32), fcent, to_face))
+            parts.append((unique, np.full(len(unique), npf, dtype=np.int32), fcent))
             shift += len(unique)
         cat0 = lambda i: np.concatenate([p[i] for p in parts], axis=0)
-        cat1 = lambda i: np.concatenate([p[i] for p in parts], axis=1)
-        return (cat0(0).astype(np.int32), cat1(1).astype(np.int32), cat1(2), cat1(3),
-                cat0(4), cat0(5), cat1(6))
+        return (cat0(0).astype(np.int32), cell_face_ids.astype(np.int32), area, normal,
+                cat0(1), cat0(2), to_face)
 
     def get_mesh_properties(self):
         unique_faces, cell_face_ids, area, normal, nodes_per_face, face_centroid, to_face = self.get_faces()
@@ -273,7 +360,12 @@ class Mesh:
         # every unique face occurs once (boundary) or twice (internal) in the (C,F)
         # table; a stable sort of the flat table puts the lower cell id first
         flat = cell_face_ids.ravel().astype(np.int64)
-        order = np.argsort(flat, kind="stable")
+        valid = flat >= 0
+        if valid.all():
+            order = np.argsort(flat, kind="stable")
+        else:
+            vidx = np.nonzero(valid)[0]
+            order = vidx[np.argsort(flat[vidx], kind="stable")]
         sf = flat[order]
         counts = np.bincount(sf, minlength=K)
         if np.any(counts > 2) or np.any(counts == 0):
@@ -304,10 +396,13 @@ class Mesh:
         faces.is_boundary = (~internal).astype(np.uint8)
         faces.adjacent_cells = np.stack([own_cell, nb_cell], axis=1).astype(fi)
         faces.cell_face_index = np.stack([own_slot, nb_slot], axis=1).astype(fi)
-        dist = np.full((K, 3), -1.0, dtype=np.float64)
+        # owner -> neighbour centroid vector, the difference of the float32 centroids
+        # taken in float32 as the reference takes it (mesh.py:276)
+        dist = np.full((K, 3), -1.0, dtype=ff)
         ii = np.nonzero(internal)[0]
-        dist[ii] = self._centroids64[nb_cell[ii]] - self._centroids64[own_cell[ii]]
-        faces.distance = dist.astype(ff)
+        c32 = self._centroids64.astype(ff)
+        dist[ii] = c32[nb_cell[ii]] - c32[own_cell[ii]]
+        faces.distance = dist
         face_ids = np.arange(K, dtype=fi)
         faces.boundary_face_ids = face_ids[~internal]
         faces.internal_face_ids = face_ids[internal]
@@ -326,13 +421,15 @@ class Mesh:
         cells.cell_centroid_to_face_centroid = to_face.astype(ff)
         cells.neighbors = neighbors.astype(fi)
         cells.face_side = face_side.astype(fi)
+        cells.slot_valid = (cell_face_ids >= 0)
+        cells.cell_types = self.cell_types
         cells.nnz_per_cell = (1 + (neighbors != -1).sum(axis=1)).astype(fi)
         m = neighbors != -1
         cells.face_offset_index = (np.cumsum(m, axis=1) * m).astype(fi)
         # volume by the divergence theorem over the fan-triangulated faces
         # (equal to VTK's cell size for cells with planar faces)
         fc_vec = (normal * area[..., None])  # outward vector area per slot
-        vol = (np.einsum("cfk,cfk->c", fc_vec, face_centroid[cell_face_ids])) / 3.0
+        vol = (np.einsum("cfk,cfk->c", fc_vec, face_centroid[np.maximum(cell_face_ids, 0)])) / 3.0
         cells.volumes = np.abs(vol).astype(ff)
         self._geometry64 = dict(area=area, normal=normal, to_face=to_face, face_centroid=face_centroid,
                                 volume=np.abs(vol), centroid=self._centroids64)
