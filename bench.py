@@ -59,9 +59,12 @@ def build_mesh(workload):
     from warpcfd_gb300.preprocess import (Mesh, create_2D_grid, create_3D_grid, create_cylinder_channel_grid,
                                           define_boundary_walls, define_cylinder_group)
 
+    import torch
+    # the large meshes go through the GPU mesh pass (bit-identical topology to the host pass)
+    dev = "cuda" if torch.cuda.is_available() else None
     if workload == "cylinder":
         g, info = create_cylinder_channel_grid(scale=1.625, jitter=0.1, seed=0)
-        m = Mesh(g)
+        m = Mesh(g, device=dev)
         define_boundary_walls(m)
         define_cylinder_group(m, info["cylinder"])
         return m
@@ -70,7 +73,7 @@ def build_mesh(workload):
     elif workload == "cavity":
         m = Mesh(create_2D_grid((0, 0, 0), 64, 64, 1.0, 1.0, 0.1))
     elif workload == "cavity3d":
-        m = Mesh(create_3D_grid((0, 0, 0), 128, 128, 128, 1.0, 1.0, 1.0))
+        m = Mesh(create_3D_grid((0, 0, 0), 128, 128, 128, 1.0, 1.0, 1.0), device=dev)
     else:
         raise ValueError(workload)
     define_boundary_walls(m)

@@ -349,6 +349,53 @@ int wcfd_batch_simple_iteration(const wcfd_case* cases, int32_t n_cases, const w
 /* Message of the last failed batched call on this thread. */
 const char* wcfd_batch_last_error(void);
 
+/* ---------------------------------------------------------------- mesh pass on the device
+ * The preprocessing of warp_cfd/preprocess/mesh.py:64-302 (Mesh.get_faces and
+ * Mesh.get_mesh_properties) for large meshes: face matching and geometry on the GPU, the
+ * topology bit-identical to the host pass (faces numbered triangles first, then quads,
+ * each set in lexicographic order of the sorted node ids; owner = lower cell id).  Cells of
+ * mixed types (hexahedra, wedges, tetrahedra) are allowed; slots past a cell's own faces are
+ * null (face id -1, zero geometry). */
+typedef struct wcfd_mesh_cells {
+    int32_t n_cells;          /* C                                                       */
+    int32_t n_points;         /* P                                                       */
+    int32_t faces_per_cell;   /* F: the largest face count of the cell types present     */
+    int32_t tri_slots;        /* the largest number of triangular faces of one cell (0: none) */
+    int32_t quad_slots;       /* the largest number of quadrilateral faces of one cell   */
+    int32_t pad_;
+    const double*  points;    /* [P*3]                                                   */
+    const int32_t* cells;     /* [C*8] node ids in VTK order, -1 past the cell's nodes   */
+    const int32_t* cell_type; /* [C] VTK type: 10 tetra, 12 hexahedron, 13 wedge          */
+} wcfd_mesh_cells;
+
+typedef struct wcfd_mesh_faces {  /* device outputs; K = n_faces[0] + n_faces[1] */
+    int32_t* cell_faces;      /* [C*F] face id per (cell, slot); -1 on null slots        */
+    int32_t* unique_faces;    /* [K*node_width] sorted node ids, -1 padded (faces.unique_faces) */
+    int32_t* face_nodes;      /* [K] nodes per face (faces.num_nodes)                    */
+    int32_t* face_cells;      /* [K*2] owner, neighbour (-1 on boundary faces)           */
+    int32_t* face_slots;      /* [K*2] the face's slot in the owner, neighbour (-1)       */
+    double*  centroid;        /* [C*3] node mean                                          */
+    double*  volume;          /* [C]   divergence theorem over the fan-triangulated faces */
+    double*  area;            /* [C*F] fan-triangulated area (mesh.py:161-183)            */
+    double*  normal;          /* [C*F*3] outward unit normal                              */
+    double*  to_face;         /* [C*F*3] cell centroid -> face centroid                    */
+    double*  face_centroid;   /* [K*3] node mean                                          */
+    int32_t  node_width;      /* 4 when the mesh has quads, else 3                        */
+    int32_t  pad_;
+} wcfd_mesh_faces;
+
+/* Device workspace the two calls below need (0 on a bad argument). */
+size_t wcfd_mesh_workspace_bytes(const wcfd_mesh_cells* m);
+/* Match faces: keys, per-node buckets, counts.  Synchronizes the stream and returns the
+ * number of triangular and of quadrilateral faces in n_faces[0..1] (host memory). */
+int wcfd_mesh_match_faces(const wcfd_mesh_cells* m, void* workspace, size_t workspace_bytes, int32_t* n_faces,
+                          void* stream);
+/* Write the topology and geometry of a matched mesh into caller-allocated arrays. */
+int wcfd_mesh_emit(const wcfd_mesh_cells* m, void* workspace, size_t workspace_bytes, const int32_t* n_faces,
+                   const wcfd_mesh_faces* out, void* stream);
+/* Message of the last failed mesh call on this thread. */
+const char* wcfd_mesh_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

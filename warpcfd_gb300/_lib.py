@@ -89,6 +89,18 @@ class BatchDims_t(ct.Structure):
                 ("cluster_size", ct.c_int32), ("field_block", ct.c_int32)]
 
 
+class MeshCells_t(ct.Structure):
+    _fields_ = [("n_cells", ct.c_int32), ("n_points", ct.c_int32), ("faces_per_cell", ct.c_int32),
+                ("tri_slots", ct.c_int32), ("quad_slots", ct.c_int32), ("pad_", ct.c_int32),
+                ("points", vp), ("cells", vp), ("cell_type", vp)]
+
+
+class MeshFaces_t(ct.Structure):
+    _fields_ = [("cell_faces", vp), ("unique_faces", vp), ("face_nodes", vp), ("face_cells", vp),
+                ("face_slots", vp), ("centroid", vp), ("volume", vp), ("area", vp), ("normal", vp),
+                ("to_face", vp), ("face_centroid", vp), ("node_width", ct.c_int32), ("pad_", ct.c_int32)]
+
+
 # name -> (restype, argtypes)
 _SIGS = {
     "wcfd_version": (ct.c_int, []),
@@ -125,6 +137,11 @@ _SIGS = {
     "wcfd_convergence_norms": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, vp, vp, vp, vp, vp, vp, vp]),
     "wcfd_batch_simple_iteration": (ct.c_int, [vp, ct.c_int32, ct.POINTER(BatchDims_t), vp]),
     "wcfd_batch_last_error": (ct.c_char_p, []),
+    "wcfd_mesh_workspace_bytes": (ct.c_size_t, [ct.POINTER(MeshCells_t)]),
+    "wcfd_mesh_match_faces": (ct.c_int, [ct.POINTER(MeshCells_t), vp, ct.c_size_t, ct.POINTER(ct.c_int32), vp]),
+    "wcfd_mesh_emit": (ct.c_int, [ct.POINTER(MeshCells_t), vp, ct.c_size_t, ct.POINTER(ct.c_int32),
+                                  ct.POINTER(MeshFaces_t), vp]),
+    "wcfd_mesh_last_error": (ct.c_char_p, []),
 }
 
 EXPORTED = tuple(_SIGS.keys())

@@ -208,11 +208,14 @@ class Mesh:
     a pyvista grid, or :class:`UnstructuredGrid`.  A grid of one cell type is handled as
     the reference handles it (mesh.py:17-43); a grid that mixes types also needs the
     flat ``cells`` and ``celltypes`` arrays, and then ``cells`` is (C, 8) padded with -1,
-    ``cell_types`` the VTK type per cell and ``cellType`` ('MIXED', 0).
+    ``cell_types`` the VTK type per cell and ``cellType`` ('MIXED', 0).  ``device`` (a
+    CUDA device) runs the face matching and the geometry on the GPU (libwcfd's mesh pass,
+    for meshes of millions of cells) with bit-identical topology.
     """
 
-    def __init__(self, grid, dtype=np.float32) -> None:
+    def __init__(self, grid, dtype=np.float32, device=None) -> None:
         cells_dict = grid.cells_dict
+        self.device = device
         self.float_dtype = np.float32
         self.int_dtype = np.int32
         self.dtype = dtype
@@ -228,9 +231,6 @@ class Mesh:
             self.cellType = (CELL_TYPE_NAMES[celltype], celltype)
             self.cells = np.asarray(cells_dict[celltype], dtype=self.int_dtype)
             self.cell_types = np.full(self.cells.shape[0], celltype, dtype=np.int32)
-            cells64 = self.cells.astype(np.int64)
-            # VTK's cell centre of a linear cell is its parametric centre = node mean
-            self._centroids64 = points[cells64].mean(axis=1)
         else:
             if not (hasattr(grid, "cells") and hasattr(grid, "celltypes")):
                 raise AssertionError("a mixed-type grid needs its flat cells and celltypes arrays")
@@ -238,14 +238,23 @@ class Mesh:
             self.cellType = ("MIXED", 0)
             self.cells = conn.astype(self.int_dtype)
             self.cell_types = ctypes.astype(np.int32)
-            real = conn >= 0
-            pts = points[np.maximum(conn, 0)] * real[..., None]
-            self._centroids64 = pts.sum(axis=1) / real.sum(axis=1)[:, None]
-        self.cell_centroids = self._centroids64.astype(self.float_dtype)
+        if device is None:
+            self._centroids64 = self._host_centroids()
+            self.cell_centroids = self._centroids64.astype(self.float_dtype)
         self.groups: dict[str, group] = {}
         self.gridType = "Unstructured"
         self.face_properties, self.cell_properties = self.get_mesh_properties()
         self.cell_volumes = self.cell_properties.volumes
+
+    def _host_centroids(self):
+        """VTK's cell centre of a linear cell: its parametric centre = the node mean."""
+        points = self._nodes64
+        if self.cellType[1] != 0:
+            return points[self.cells.astype(np.int64)].mean(axis=1)
+        conn = self.cells.astype(np.int64)
+        real = conn >= 0
+        pts = points[np.maximum(conn, 0)] * real[..., None]
+        return pts.sum(axis=1) / real.sum(axis=1)[:, None]
 
     @classmethod
     def from_arrays(cls, nodes, cells, cell_type=HEXAHEDRON):
@@ -351,11 +360,21 @@ class Mesh:
                 cat0(1), cat0(2), to_face)
 
     def get_mesh_properties(self):
+        """faces_data, cells_data (mesh.py:186-302); face matching and geometry on the host,
+        or on ``device`` (a CUDA device) through libwcfd's mesh pass."""
+        if self.device is not None:
+            from .device_pass import device_topology
+            raw = device_topology(self, self.device)
+            self._centroids64 = raw["centroid"]
+            self.cell_centroids = self._centroids64.astype(self.float_dtype)
+        else:
+            raw = self._host_topology()
+        return self._assemble(raw)
+
+    def _host_topology(self):
         unique_faces, cell_face_ids, area, normal, nodes_per_face, face_centroid, to_face = self.get_faces()
         C, F = cell_face_ids.shape
         K = unique_faces.shape[0]
-        fi = self.int_dtype
-        ff = self.float_dtype
 
         # every unique face occurs once (boundary) or twice (internal) in the (C,F)
         # table; a stable sort of the flat table puts the lower cell id first
@@ -380,6 +399,20 @@ class Mesh:
         nb_slot = np.where(internal, second_pos % F, -1)
         if np.any(internal & (nb_cell == own_cell)):
             raise AssertionError("a cell shares a face with itself")
+        return dict(unique_faces=unique_faces, cell_face_ids=cell_face_ids, area=area, normal=normal,
+                    nodes_per_face=nodes_per_face, face_centroid=face_centroid, to_face=to_face,
+                    own_cell=own_cell, own_slot=own_slot, nb_cell=nb_cell, nb_slot=nb_slot, volume=None)
+
+    def _assemble(self, raw):
+        unique_faces, cell_face_ids = raw["unique_faces"], raw["cell_face_ids"]
+        area, normal, to_face = raw["area"], raw["normal"], raw["to_face"]
+        nodes_per_face, face_centroid = raw["nodes_per_face"], raw["face_centroid"]
+        own_cell, own_slot, nb_cell, nb_slot = raw["own_cell"], raw["own_slot"], raw["nb_cell"], raw["nb_slot"]
+        C, F = cell_face_ids.shape
+        K = unique_faces.shape[0]
+        fi = self.int_dtype
+        ff = self.float_dtype
+        internal = nb_cell >= 0
 
         faces = faces_data()
         cells = cells_data()
@@ -428,9 +461,12 @@ class Mesh:
         cells.face_offset_index = (np.cumsum(m, axis=1) * m).astype(fi)
         # volume by the divergence theorem over the fan-triangulated faces
         # (equal to VTK's cell size for cells with planar faces)
-        fc_vec = (normal * area[..., None])  # outward vector area per slot
-        vol = (np.einsum("cfk,cfk->c", fc_vec, face_centroid[np.maximum(cell_face_ids, 0)])) / 3.0
-        cells.volumes = np.abs(vol).astype(ff)
+        if raw["volume"] is None:
+            fc_vec = (normal * area[..., None])  # outward vector area per slot
+            vol = np.abs(np.einsum("cfk,cfk->c", fc_vec, face_centroid[np.maximum(cell_face_ids, 0)]) / 3.0)
+        else:
+            vol = raw["volume"]
+        cells.volumes = vol.astype(ff)
         self._geometry64 = dict(area=area, normal=normal, to_face=to_face, face_centroid=face_centroid,
-                                volume=np.abs(vol), centroid=self._centroids64)
+                                volume=vol, centroid=self._centroids64)
         return faces, cells
