@@ -176,6 +176,14 @@ typedef struct wcfd_case {
 /* ------------------------------------------------------------------ info */
 int         wcfd_version(void);
 const char* wcfd_last_error(void);
+
+/* Self-check of the grid barrier the grid-cooperative Krylov kernels use (no reference
+ * counterpart): `phases` barriers of two sums over a full cooperative grid, every block
+ * checking the sums against their closed form.  skip_block >= 0 makes that block return
+ * before its first arrival, so the others' bounded waits run out (a failure made without a
+ * fault).  Synchronizes the stream.  result (host): [0] the kernel's error word (WCFD_OK or
+ * WCFD_BARRIER_TIMEOUT), [1] 1 if a block received wrong sums, [2] blocks in the grid. */
+int wcfd_grid_barrier_check(int32_t skip_block, int32_t phases, int32_t* result, void* stream);
 /* floats of wcfd_krylov_ws.vec needed for a C-row system with ncomp components */
 int64_t     wcfd_krylov_workspace_floats(int32_t n_cells, int32_t ncomp);
 

@@ -228,6 +228,52 @@ int wcfd_set_krylov_path(int32_t path) {
 
 const char* wcfd_last_error(void) { return g_last_error; }
 
+int wcfd_grid_barrier_check(int32_t skip_block, int32_t phases, int32_t* result, void* stream) {
+    RET_IF(!result || phases < 1 || phases > 100000, WCFD_ERR_ARGUMENT, "bad phases or null result");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const void* fn = barrier_check_kernel_ptr();
+    const int cap = coop_capacity(fn, 0);
+    LAUNCH_CHECK("occupancy query");
+    RET_IF(cap <= 0, WCFD_ERR_CUDA, "barrier check kernel cannot be resident");
+    RET_IF(skip_block >= cap, WCFD_ERR_ARGUMENT, "skip_block beyond the grid");
+    unsigned* words = nullptr;
+    double* partials = nullptr;
+    int* bad = nullptr;
+    int rc = WCFD_OK;
+    if (cudaMalloc(&words, WCFD_BARRIER_WORDS * sizeof(unsigned)) != cudaSuccess ||
+        cudaMalloc(&partials, 8 * WCFD_MAX_BLOCKS * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&bad, sizeof(int)) != cudaSuccess) {
+        rc = set_error(WCFD_ERR_CUDA, "barrier check: allocation failed");
+    }
+    if (rc == WCFD_OK && (cudaMemsetAsync(words, 0, WCFD_BARRIER_WORDS * sizeof(unsigned), st) != cudaSuccess ||
+                          cudaMemsetAsync(bad, 0, sizeof(int), st) != cudaSuccess))
+        rc = set_error(WCFD_ERR_CUDA, "barrier check: memset failed");
+    if (rc == WCFD_OK) {
+        GridCtl g;
+        g.partials = partials;
+        g.flags = words;
+        g.err = reinterpret_cast<int*>(words + WCFD_MAX_BLOCKS);
+        int skip = skip_block, ph = phases;
+        void* args[] = {&g, &skip, &ph, &bad};
+        int host[2] = {0, 0};
+        if (cudaLaunchCooperativeKernel(fn, dim3(cap), dim3(kSolverBlock), args, 0, st) != cudaSuccess ||
+            cudaMemcpyAsync(&host[0], g.err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaMemcpyAsync(&host[1], bad, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) {
+            rc = check_launch("barrier check");
+            if (rc == WCFD_OK) rc = set_error(WCFD_ERR_CUDA, "barrier check failed");
+        } else {
+            result[0] = host[0];
+            result[1] = host[1];
+            result[2] = cap;
+        }
+    }
+    cudaFree(words);
+    cudaFree(partials);
+    cudaFree(bad);
+    return rc;
+}
+
 int64_t wcfd_krylov_workspace_floats(int32_t n_cells, int32_t ncomp) {
     if (n_cells <= 0 || (ncomp != 1 && ncomp != 3)) return -1;
     return ncomp == 1 ? 6LL * n_cells : 27LL * n_cells;

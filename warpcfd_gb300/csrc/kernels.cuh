@@ -54,6 +54,7 @@ struct KrylovArgs {
 };
 // kernel instantiations for off-diagonal width W (0..6), nullptr otherwise
 const void* cg_kernel_for(int W);
+const void* barrier_check_kernel_ptr();
 const void* bicgstab_kernel_for(int W);
 const void* cg_cluster_kernel_for(int W, int R);
 const void* cg_cluster_batched_for(int W, int R);

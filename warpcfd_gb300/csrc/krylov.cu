@@ -90,7 +90,7 @@ __device__ void write_stats(const KrylovArgs& a, const KScalars& sc) {
 // coefficient and gather loads are in flight: the pass is bound by memory latency, not
 // by bandwidth, at one row per thread.
 template <int W>
-__global__ void __launch_bounds__(BS, 3) cg_kernel(KrylovArgs a) {
+__global__ void __launch_bounds__(BS, 1) cg_kernel(KrylovArgs a) {
     __shared__ KScalars sc;
     const int C = a.m.n_cells;
     float* r = a.ws;
@@ -459,6 +459,28 @@ const void* residual64_kernel_for(int W) {
         default: return nullptr;
     }
 }
+
+// Self-check of the grid barrier: `phases` barriers of two sums over all blocks; every block
+// checks the sums it receives against their closed form and ORs 1 into *bad on a mismatch.
+// With skip >= 0 that block returns before it arrives at the first barrier, so every other
+// block's wait runs out: they record WCFD_BARRIER_TIMEOUT in the error word and return (a
+// failure made without a fault: nothing ever sets the count they wait for).
+__global__ void __launch_bounds__(BS, 1) barrier_check_kernel(GridCtl g, int skip, int phases, int* bad) {
+    if ((int)blockIdx.x == skip) return;
+    unsigned phase = 0;
+    const float G = (float)gridDim.x;
+    for (int p = 0; p < phases; ++p) {
+        ff acc[2] = {ff{(float)(blockIdx.x + 1 + p), 0.0f}, ff{1.0f, 0.0f}};
+        ff out[2];
+        if (threadIdx.x != 0) acc[0] = acc[1] = ff_zero();
+        if (!grid_sync<2, BS>(g, acc, out, ++phase)) return;
+        const float want0 = G * (G + 1.0f) * 0.5f + G * (float)p;  // exact below 2^24
+        if (threadIdx.x == 0 && (ff_to_double(out[0]) != (double)want0 || ff_to_double(out[1]) != (double)G))
+            atomicOr(bad, 1);
+    }
+}
+
+const void* barrier_check_kernel_ptr() { return (const void*)barrier_check_kernel; }
 
 const void* cg_kernel_for(int W) {
     switch (W) {
