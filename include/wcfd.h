@@ -335,6 +335,9 @@ typedef struct wcfd_batch_dims {
     int32_t field_block;     /* threads per block of the field/assembly kernels: 0 = 256,
                                 else 64..512 in steps of 32 (the result does not depend
                                 on it: those kernels compute each face or cell alone)  */
+    int32_t explicit_terms;  /* OR of the cases' wcfd_params.explicit_terms: non-zero
+                                selects the assembly kernels with those terms compiled in */
+    int32_t pad_;
 } wcfd_batch_dims;
 
 /* Cluster size wcfd_batch_simple_iteration would pick for these dims (0 = no cluster

@@ -38,17 +38,18 @@ def test_struct_layout_matches_header(tmp_path):
 
     prog = tmp_path / "layout.c"
     prog.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "wcfd.h"\nint main(){printf("%zu %zu %zu '
-                    '%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(wcfd_mesh), sizeof(wcfd_bc), '
+                    '%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(wcfd_mesh), sizeof(wcfd_bc), '
                     'sizeof(wcfd_state), sizeof(wcfd_system), sizeof(wcfd_krylov_ws), sizeof(wcfd_solve_stats), '
                     'sizeof(wcfd_params), sizeof(wcfd_case), offsetof(wcfd_case, prm), offsetof(wcfd_case, stats), '
-                    'sizeof(wcfd_mesh_cells), sizeof(wcfd_mesh_faces), offsetof(wcfd_mesh_faces, node_width));}\n')
+                    'sizeof(wcfd_mesh_cells), sizeof(wcfd_mesh_faces), offsetof(wcfd_mesh_faces, node_width), '
+                    'sizeof(wcfd_batch_dims));}\n')
     exe = tmp_path / "layout"
     subprocess.run(["gcc", f"-I{os.path.join(ROOT, 'include')}", str(prog), "-o", str(exe)], check=True)
     got = list(map(int, subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()))
     want = [ct.sizeof(t) for t in (_lib.Mesh_t, _lib.BC_t, _lib.State_t, _lib.System_t, _lib.KrylovWS_t,
                                    _lib.Stats_t, _lib.Params_t, _lib.Case_t)]
     want += [_lib.Case_t.prm.offset, _lib.Case_t.stats.offset, ct.sizeof(_lib.MeshCells_t),
-             ct.sizeof(_lib.MeshFaces_t), _lib.MeshFaces_t.node_width.offset]
+             ct.sizeof(_lib.MeshFaces_t), _lib.MeshFaces_t.node_width.offset, ct.sizeof(_lib.BatchDims_t)]
     assert got == want
 
 

@@ -107,3 +107,35 @@ def test_graph_replay_field_block_and_autotune_keep_results():
         b2.step()
     for i, (m, _) in enumerate(tuned):
         assert np.array_equal(fields(m), want[i]), i
+
+
+def test_batch_with_explicit_terms_matches_alone():
+    """A batch whose cases use the opt-in explicit internal terms (the assembly kernels with
+    those terms compiled in): each case equals itself alone in a batch of one, bit for bit,
+    and differs from the same case without the option."""
+    from warpcfd_gb300.batch import CaseBatch
+
+    def make(xt):
+        m1, s1, _ = make_pair(cavity_mesh(16, jitter=0.15, seed=11), cavity_bc, correction=True)
+        m2, s2, _ = make_pair(cavity_mesh(12, jitter=0.1, seed=3), cavity_bc, correction=True)
+        for s in (s1, s2):
+            s.explicit_internal_terms = xt
+        return [(m1, s1), (m2, s2)]
+
+    mix = make(True)
+    batch = CaseBatch([s for _, s in mix])
+    assert batch.dims.explicit_terms == 5
+    for _ in range(4):
+        batch.step()
+    got = [fields(m) for m, _ in mix]
+    for i, (m, s) in enumerate(make(True)):
+        alone = CaseBatch([s], cluster_size=batch.cluster_size)
+        for _ in range(4):
+            alone.step()
+        assert np.array_equal(fields(m), got[i]), i
+    plain = make(False)
+    pb = CaseBatch([s for _, s in plain], cluster_size=batch.cluster_size)
+    assert pb.dims.explicit_terms == 0
+    for _ in range(4):
+        pb.step()
+    assert not np.array_equal(fields(plain[0][0]), got[0])

@@ -66,11 +66,18 @@ class CaseBatch:
         """(Re)build the device case table from the solvers' current parameters."""
         n = len(self.solvers)
         arr = (_lib.Case_t * n)()
+        xt = 0
         for i, s in enumerate(self.solvers):
             c = _lib.Case_t.from_buffer_copy(s.case_struct())
             c.stats = self.stats.data_ptr() + i * 2 * _lib.STATS_BYTES
             c.events = None
             arr[i] = c
+            xt |= int(c.prm.explicit_terms)
+        if xt != self.dims.explicit_terms:
+            # the assembly kernels the step launches depend on it: a captured graph is stale
+            self.dims.explicit_terms = xt
+            self._graph = None
+            self._graph_steps = 0
         host = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8)
         self.table.copy_(host.to(self.device))
 

@@ -68,6 +68,9 @@ __device__ __forceinline__ void explicit_internal_terms(const wcfd_mesh& m, cons
     }
 }
 
+// XT: the opt-in explicit internal terms are compiled in (their code raises the kernel from
+// 32 to 48 registers, so the default instantiation leaves it out)
+template <bool XT>
 __device__ __forceinline__ void momentum_assemble_body(const wcfd_mesh& m, const wcfd_bc& bc, const wcfd_state& s, const wcfd_system& sys, float* __restrict__ rua, const wcfd_params& prm, int c) {
     const int C = m.n_cells;
     const float nu = prm.nu;
@@ -97,7 +100,8 @@ __device__ __forceinline__ void momentum_assemble_body(const wcfd_mesh& m, const
             dsum += w0 + dcoef;
             sys.off[(size_t)j * C + c] = w1 - dcoef;
             ++j;
-            if (prm.explicit_terms) explicit_internal_terms(m, s, k, owner_side, md, nu, prm.explicit_terms, 0, 3, b, 1.0f, -1.0f);
+            if (XT && prm.explicit_terms)
+                explicit_internal_terms(m, s, k, owner_side, md, nu, prm.explicit_terms, 0, 3, b, 1.0f, -1.0f);
         } else {
             const int br = __ldg(m.face_brow + k);
             const uchar4 t = __ldg(reinterpret_cast<const uchar4*>(bc.type) + br);
@@ -144,12 +148,21 @@ __device__ __forceinline__ void momentum_assemble_body(const wcfd_mesh& m, const
     rua[c] = V / (d[0] * prm.rho);
 }
 
+template <bool XT>
 __global__ void __launch_bounds__(kBlock) momentum_assemble_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s,
                                                                    wcfd_system sys, float* __restrict__ rua,
                                                                    wcfd_params prm) {
     const int c = blockIdx.x * kBlock + threadIdx.x;
     if (c >= m.n_cells) return;
-    momentum_assemble_body(m, bc, s, sys, rua, prm, c);
+    momentum_assemble_body<XT>(m, bc, s, sys, rua, prm, c);
+}
+
+void launch_momentum_assemble(bool xt, int grid, cudaStream_t st, const wcfd_mesh& m, const wcfd_bc& bc,
+                              const wcfd_state& s, const wcfd_system& sys, float* rua, const wcfd_params& prm) {
+    if (xt)
+        momentum_assemble_kernel<true><<<grid, kBlock, 0, st>>>(m, bc, s, sys, rua, prm);
+    else
+        momentum_assemble_kernel<false><<<grid, kBlock, 0, st>>>(m, bc, s, sys, rua, prm);
 }
 
 // Implicit relaxation of an assembled system on its diagonal (equation_kernels.py:128-152):
@@ -185,6 +198,7 @@ __global__ void replace_row_kernel(int C, int W, wcfd_system sys, int row, float
 //   boundary gradient: rhs -= rUA_f g A
 // then rhs += div(HbyA) (incompressible.py:137) and, for the reference cell, the row
 // becomes identity with rhs = value (equation_kernels.py:155-175; its column stays).
+template <bool XT>
 __device__ __forceinline__ void pressure_assemble_body(const wcfd_mesh& m, const wcfd_bc& bc, const wcfd_state& s, const wcfd_system& sys, const float* __restrict__ rua_faces, const float* __restrict__ div, const wcfd_params& prm, int c) {
     const int C = m.n_cells;
     float d = 0.0f, b = 0.0f;
@@ -201,7 +215,7 @@ __device__ __forceinline__ void pressure_assemble_body(const wcfd_mesh& m, const
             d -= coef;
             sys.off[(size_t)j * C + c] = ref ? 0.0f : coef;
             ++j;
-            if (prm.explicit_terms & 4)  // opt-in non-orthogonal explicit part (see momentum)
+            if (XT && (prm.explicit_terms & 4))  // opt-in non-orthogonal explicit part (see momentum)
                 explicit_internal_terms(m, s, k, sk >= 0, 0.0f, rua_faces[k], 4, 3, 1, &b, 0.0f, 1.0f);
         } else {
             const int br = __ldg(m.face_brow + k);
@@ -225,13 +239,23 @@ __device__ __forceinline__ void pressure_assemble_body(const wcfd_mesh& m, const
     sys.rhs[c] = b;
 }
 
+template <bool XT>
 __global__ void __launch_bounds__(kBlock) pressure_assemble_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s,
                                                                    wcfd_system sys,
                                                                    const float* __restrict__ rua_faces,
                                                                    const float* __restrict__ div, wcfd_params prm) {
     const int c = blockIdx.x * kBlock + threadIdx.x;
     if (c >= m.n_cells) return;
-    pressure_assemble_body(m, bc, s, sys, rua_faces, div, prm, c);
+    pressure_assemble_body<XT>(m, bc, s, sys, rua_faces, div, prm, c);
+}
+
+void launch_pressure_assemble(bool xt, int grid, cudaStream_t st, const wcfd_mesh& m, const wcfd_bc& bc,
+                              const wcfd_state& s, const wcfd_system& sys, const float* rua_faces, const float* div,
+                              const wcfd_params& prm) {
+    if (xt)
+        pressure_assemble_kernel<true><<<grid, kBlock, 0, st>>>(m, bc, s, sys, rua_faces, div, prm);
+    else
+        pressure_assemble_kernel<false><<<grid, kBlock, 0, st>>>(m, bc, s, sys, rua_faces, div, prm);
 }
 
 // y = A x on the mesh pattern; NC = 1 (scalar) or 3 (momentum: shared off-diagonals,
@@ -267,18 +291,34 @@ void launch_spmv(const wcfd_mesh& m, wcfd_system A, const float* x, float* y, cu
 // Batched assembly over a device case table (blockIdx.y = case).
 namespace wcfd {
 
+template <bool XT>
 __global__ void __launch_bounds__(kMaxFieldBlock) momentum_assemble_batched(const wcfd_case* __restrict__ cases) {
     const wcfd_case& c = cases[blockIdx.y];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.mesh.n_cells) return;
-    momentum_assemble_body(c.mesh, c.bc, c.state, c.mom, c.rua, c.prm, i);
+    momentum_assemble_body<XT>(c.mesh, c.bc, c.state, c.mom, c.rua, c.prm, i);
 }
 
+template <bool XT>
 __global__ void __launch_bounds__(kMaxFieldBlock) pressure_assemble_batched(const wcfd_case* __restrict__ cases) {
     const wcfd_case& c = cases[blockIdx.y];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= c.mesh.n_cells) return;
-    pressure_assemble_body(c.mesh, c.bc, c.state, c.pres, c.rua_faces, c.div, c.prm, i);
+    pressure_assemble_body<XT>(c.mesh, c.bc, c.state, c.pres, c.rua_faces, c.div, c.prm, i);
+}
+
+void launch_assemble_batched(bool pressure, bool xt, dim3 grid, int block, cudaStream_t st, const wcfd_case* cases) {
+    if (pressure) {
+        if (xt)
+            pressure_assemble_batched<true><<<grid, block, 0, st>>>(cases);
+        else
+            pressure_assemble_batched<false><<<grid, block, 0, st>>>(cases);
+    } else {
+        if (xt)
+            momentum_assemble_batched<true><<<grid, block, 0, st>>>(cases);
+        else
+            momentum_assemble_batched<false><<<grid, block, 0, st>>>(cases);
+    }
 }
 
 }  // namespace wcfd

@@ -165,7 +165,7 @@ extern "C" int wcfd_batch_simple_iteration(const wcfd_case* cases, int32_t n_cas
     gradient_batched<<<gc, fb, 0, st>>>(cases, WCFD_ALL, 0);
     BCHECK("gradient_batched");
     // :102-116
-    momentum_assemble_batched<<<gc, fb, 0, st>>>(cases);
+    launch_assemble_batched(false, d.explicit_terms != 0, gc, fb, st, cases);
     BCHECK("momentum_assemble_batched");
     int csv = cs;
     void* bargs[] = {(void*)&cases, &csv};
@@ -183,7 +183,7 @@ extern "C" int wcfd_batch_simple_iteration(const wcfd_case* cases, int32_t n_cas
             BCHECK("face_pass_batched");
             gradient_batched<<<gc, fb, 0, st>>>(cases, WCFD_ALL, 1);
             BCHECK("gradient_batched");
-            pressure_assemble_batched<<<gc, fb, 0, st>>>(cases);
+            launch_assemble_batched(true, (d.explicit_terms & 4) != 0, gc, fb, st, cases);
             BCHECK("pressure_assemble_batched");
             void* cargs[] = {(void*)&cases, &csv};
             rc = launch_cluster(cg_fn, n_cases, cs, smem, st, cargs);

@@ -360,8 +360,8 @@ int wcfd_assemble_momentum(const wcfd_case* c, void* stream) {
     if (rc) return rc;
     RET_IF(!c->mom.diag || !c->mom.off || !c->mom.rhs || !c->rua, WCFD_ERR_ARGUMENT, "null momentum array");
     RET_IF(c->prm.rho == 0.0f || (!c->prm.steady && c->prm.dt <= 0.0f), WCFD_ERR_ARGUMENT, "bad rho or dt");
-    momentum_assemble_kernel<<<grid_for(c->mesh.n_cells), kBlock, 0, S(stream)>>>(c->mesh, c->bc, c->state, c->mom,
-                                                                                 c->rua, c->prm);
+    launch_momentum_assemble(c->prm.explicit_terms != 0, grid_for(c->mesh.n_cells), S(stream), c->mesh, c->bc,
+                             c->state, c->mom, c->rua, c->prm);
     LAUNCH_CHECK("momentum_assemble_kernel");
     return WCFD_OK;
 }
@@ -373,8 +373,8 @@ int wcfd_assemble_pressure(const wcfd_case* c, void* stream) {
     RET_IF(!c->pres.diag || !c->pres.off || !c->pres.rhs || !c->rua_faces || !c->div, WCFD_ERR_ARGUMENT,
            "null pressure array");
     RET_IF(c->prm.ref_cell >= c->mesh.n_cells, WCFD_ERR_ARGUMENT, "reference cell out of range");
-    pressure_assemble_kernel<<<grid_for(c->mesh.n_cells), kBlock, 0, S(stream)>>>(c->mesh, c->bc, c->state, c->pres,
-                                                                                 c->rua_faces, c->div, c->prm);
+    launch_pressure_assemble((c->prm.explicit_terms & 4) != 0, grid_for(c->mesh.n_cells), S(stream), c->mesh, c->bc,
+                             c->state, c->pres, c->rua_faces, c->div, c->prm);
     LAUNCH_CHECK("pressure_assemble_kernel");
     return WCFD_OK;
 }

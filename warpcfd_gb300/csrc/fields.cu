@@ -126,10 +126,12 @@ __device__ __forceinline__ void gradient_body(const wcfd_mesh& m, const wcfd_sta
     float dv = 0.0f;
     const float4* slots = reinterpret_cast<const float4*>(m.cell_slot);
     for (int f = 0; f < m.faces_per_cell; ++f) {
+        // a null slot (mixed meshes) reads face 0 and adds nothing: its vector is zero and
+        // its flux is masked; a select, not a branch, so the loads stay uniform
         const float4 sl = __ldg(slots + (size_t)f * C + c);
         const int sk = __float_as_int(sl.w);
-        if (sk == kNullSlot) continue;
-        const int k = sk >= 0 ? sk : ~sk;
+        const bool real = sk != kNullSlot;
+        const int k = !real ? 0 : sk >= 0 ? sk : ~sk;
         const float4 fv = ld4(s.face_values + 4 * (size_t)k);
 #pragma unroll
         for (int o = 0; o < 4; ++o) {
@@ -141,7 +143,7 @@ __device__ __forceinline__ void gradient_body(const wcfd_mesh& m, const wcfd_sta
         }
         if (div) {
             const float md = s.mass_fluxes[k];
-            dv += sk >= 0 ? md : -md;
+            dv += !real ? 0.0f : sk >= 0 ? md : -md;
         }
     }
     float* gc = s.cell_gradients + 12 * (size_t)c;
@@ -188,9 +190,9 @@ __device__ __forceinline__ void div_body(const wcfd_mesh& m, const float* __rest
     float dv = 0.0f;
     for (int f = 0; f < m.faces_per_cell; ++f) {
         const int sk = __float_as_int(__ldg(&slots[(size_t)f * C + c].w));
-        if (sk == kNullSlot) continue;
-        const float md = mdot[sk >= 0 ? sk : ~sk];
-        dv += sk >= 0 ? md : -md;
+        const bool real = sk != kNullSlot;
+        const float md = mdot[!real ? 0 : sk >= 0 ? sk : ~sk];
+        dv += !real ? 0.0f : sk >= 0 ? md : -md;
     }
     div[c] = dv;
 }

@@ -19,10 +19,13 @@ __global__ void cell_to_face_kernel(wcfd_mesh m, const float* x, float* y);
 __global__ void hbya_kernel(int C, const float* grad, const float* rua, float* hbya, float* cell_values);
 __global__ void p_update_kernel(int C, const float* p_new, float* cell_values, float alpha);
 
-__global__ void momentum_assemble_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s, wcfd_system sys,
-                                         float* rua, wcfd_params prm);
-__global__ void pressure_assemble_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s, wcfd_system sys,
-                                         const float* rua_faces, const float* div, wcfd_params prm);
+// assembly launches; xt selects the kernels with the opt-in explicit internal terms
+// (wcfd_params.explicit_terms) compiled in
+void launch_momentum_assemble(bool xt, int grid, cudaStream_t st, const wcfd_mesh& m, const wcfd_bc& bc,
+                              const wcfd_state& s, const wcfd_system& sys, float* rua, const wcfd_params& prm);
+void launch_pressure_assemble(bool xt, int grid, cudaStream_t st, const wcfd_mesh& m, const wcfd_bc& bc,
+                              const wcfd_state& s, const wcfd_system& sys, const float* rua_faces, const float* div,
+                              const wcfd_params& prm);
 
 // batched forms over a device case table (blockIdx.y = case)
 __global__ void face_pass_batched(const wcfd_case* cases, uint32_t mask, uint32_t flags);
@@ -30,8 +33,7 @@ __global__ void gradient_batched(const wcfd_case* cases, uint32_t mask, int mode
 __global__ void hbya_batched(const wcfd_case* cases);
 __global__ void rua_faces_batched(const wcfd_case* cases);
 __global__ void p_update_batched(const wcfd_case* cases);
-__global__ void momentum_assemble_batched(const wcfd_case* cases);
-__global__ void pressure_assemble_batched(const wcfd_case* cases);
+void launch_assemble_batched(bool pressure, bool xt, dim3 grid, int block, cudaStream_t st, const wcfd_case* cases);
 
 // y = A x (NC = A.ncomp), launched from assemble.cu where the kernel template lives
 __global__ void relax_kernel(int C, wcfd_system sys, const float* cell_values, int field0, float a);
