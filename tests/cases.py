@@ -71,6 +71,13 @@ def mixed_cavity3d_mesh(n=6, prism_fraction=0.5, seed=0):
     return m
 
 
+def tet_cavity3d_mesh(n=4, jitter=0.0, seed=0):
+    """The 3D cavity with every hex cut into six tetrahedra."""
+    m = Mesh(create_3D_grid((0, 0, 0), n, n, n, 1.0, 1.0, 1.0, element_type="tetra", jitter=jitter, seed=seed))
+    define_boundary_walls(m)
+    return m
+
+
 def host_boundary(m, bc_fn, **kw):
     b = Boundary(FIELDS, m.groups, m.face_properties.boundary_face_ids)
     bc_fn(b, **kw)

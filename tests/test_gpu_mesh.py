@@ -24,6 +24,7 @@ GRIDS = {
     "prism2d": lambda: create_2D_grid((0, 0, 0), 12, 9, 2.0, 1.0, 0.1, element_type="wedge", jitter=0.1, seed=1),
     "mixed2d": lambda: create_2D_grid((0, 0, 0), 14, 6, 3.0, 1.0, 0.1, element_type="mixed"),
     "mixed3d": lambda: create_3D_grid((0, 0, 0), 8, 6, 5, 1.0, 1.0, 1.0, prism_fraction=0.4, seed=7),
+    "tetra3d_jitter": lambda: create_3D_grid((0, 0, 0), 6, 5, 4, 1.0, 1.0, 1.0, element_type="tetra", jitter=0.2, seed=8),
     "cylinder": lambda: create_cylinder_channel_grid(scale=0.5)[0],
 }
 

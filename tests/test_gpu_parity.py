@@ -14,7 +14,7 @@ import pytest
 import torch
 
 from tests.cases import (cavity3d_bc, cavity3d_mesh, cavity_bc, cavity_mesh, channel_bc, channel_mesh,
-                         mixed_cavity3d_mesh, prism_cavity_mesh, prism_channel_mesh)
+                         mixed_cavity3d_mesh, prism_cavity_mesh, prism_channel_mesh, tet_cavity3d_mesh)
 from tests.gpu_helpers import fields, make_pair, oracle_step, rel_l2, vel_err
 
 pytestmark = pytest.mark.gpu
@@ -601,16 +601,19 @@ def test_explicit_internal_terms_option_tracks_oracle(variant):
     assert not torch.equal(model.cell_values, m2.cell_values)
 
 
-@pytest.mark.parametrize("case", ["prism_cavity", "mixed_cavity_skew", "prism_channel", "mixed_cavity3d"])
+@pytest.mark.parametrize("case", ["prism_cavity", "mixed_cavity_skew", "prism_channel", "mixed_cavity3d",
+                                  "tet_cavity3d", "tet_cavity3d_skew"])
 def test_prism_and_mixed_meshes_track_oracle(case):
-    """Wedge meshes and mixed hex/prism meshes (null slots past a wedge's five faces):
-    the GPU step follows the oracle on the same mesh, corrected and uncorrected.  The
+    """Wedge, tetrahedral and mixed hex/prism meshes (null slots past a wedge's five
+    faces): the GPU step follows the oracle on the same mesh, corrected and uncorrected.  The
     prism channel is 5 long: on a 10-long one the oracle's own results move by 1.1e-5
     when only the summation order of its SpMV changes, above the 1e-5 bound."""
     mk = {"prism_cavity": (lambda: prism_cavity_mesh(12, "wedge"), cavity_bc, 0, 0.01, False),
           "mixed_cavity_skew": (lambda: prism_cavity_mesh(16, "mixed", jitter=0.1, seed=5), cavity_bc, 0, 0.01, True),
           "prism_channel": (lambda: prism_channel_mesh(20, 5, lx=5.0), channel_bc, None, 0.05, False),
-          "mixed_cavity3d": (lambda: mixed_cavity3d_mesh(8, 0.5, seed=2), cavity3d_bc, 0, 0.01, True)}[case]
+          "mixed_cavity3d": (lambda: mixed_cavity3d_mesh(8, 0.5, seed=2), cavity3d_bc, 0, 0.01, True),
+          "tet_cavity3d": (lambda: tet_cavity3d_mesh(5), cavity3d_bc, 0, 0.01, False),
+          "tet_cavity3d_skew": (lambda: tet_cavity3d_mesh(5, jitter=0.15, seed=6), cavity3d_bc, 0, 0.01, True)}[case]
     m = mk[0]()
     model, solver, oc = make_pair(m, mk[1], ref_cell=mk[2], nu=mk[3], correction=mk[4])
     for it in range(5):

@@ -11,7 +11,9 @@ from warpcfd_gb300.preprocess import Mesh, create_2D_grid, create_3D_grid, defin
 @pytest.mark.parametrize("make", [lambda: cavity_mesh(5), lambda: cavity_mesh(6, jitter=0.1, seed=3),
                                   lambda: cavity3d_mesh(4, jitter=0.1, seed=1), lambda: channel_mesh(7, 3),
                                   lambda: Mesh(create_2D_grid((0, 0, 0), 5, 4, 1.0, 1.0, 0.1,
-                                                              element_type="wedge", jitter=0.1, seed=2))])
+                                                              element_type="wedge", jitter=0.1, seed=2)),
+                                  lambda: Mesh(create_3D_grid((0, 0, 0), 3, 3, 2, 1.0, 1.0, 0.5, element_type="tetra",
+                                                              jitter=0.15, seed=4))])
 def test_matches_reference_loop(make):
     m = make()
     ref = reference_mesh_properties(m.nodes.astype(np.float64), m.cells)

@@ -14,7 +14,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .mesh import HEXAHEDRON, WEDGE, Mesh, UnstructuredGrid
+from .mesh import HEXAHEDRON, TETRA, WEDGE, Mesh, UnstructuredGrid
 
 
 def _hex_connectivity(nx, ny, nz):
@@ -59,6 +59,23 @@ def _cells_with_prisms(conn, split):
         flat[start[first[split]] + 1 + j] = a[:, j]
         flat[start[first[split] + 1] + 1 + j] = b[:, j]
     return flat, types
+
+
+# Kuhn subdivision of a hex into six tetrahedra around its 0-6 diagonal (VTK hex order);
+# the same diagonal direction in every cell of a lattice gives a conforming mesh
+_KUHN = np.array([[0, 1, 2, 6], [0, 2, 3, 6], [0, 3, 7, 6], [0, 7, 4, 6], [0, 4, 5, 6], [0, 5, 1, 6]])
+
+
+def _tets_of_hexes(conn, pts):
+    """(6C, 4) tetrahedra of a hex lattice, each ordered as VTK orders a tetra (nodes 0-1-2
+    counter-clockwise seen from node 3: positive signed volume), so the tetra face table
+    yields outward normals."""
+    tets = conn[:, _KUHN].reshape(-1, 4)
+    p = pts[tets]
+    vol = np.einsum("ij,ij->i", np.cross(p[:, 1] - p[:, 0], p[:, 2] - p[:, 0]), p[:, 3] - p[:, 0])
+    neg = vol < 0
+    tets[neg, 1], tets[neg, 2] = tets[neg, 2].copy(), tets[neg, 1].copy()
+    return tets
 
 
 def _lattice(origin, nx, ny, nz, lx, ly, lz):
@@ -122,18 +139,26 @@ def create_2D_grid(origin, nx, ny, dx, dy, dz=0.1, *, element_type="hex", unstru
 
 
 def create_3D_grid(origin, nx, ny, nz, lx, ly, lz, *, jitter=0.0, seed=0,
-                   prism_fraction=0.0) -> UnstructuredGrid:
+                   prism_fraction=0.0, element_type="hex") -> UnstructuredGrid:
     """Box ``lx`` x ``ly`` x ``lz`` of ``nx`` x ``ny`` x ``nz`` hexes (the 3D cavity case).
 
     ``prism_fraction`` > 0 cuts that fraction of the hexes (a seeded random choice) into
     two wedges each: a mixed hex/prism mesh.  With ``jitter`` the cut hexes' faces are no
-    longer planar, so jitter and prisms are not combined."""
+    longer planar, so jitter and prisms are not combined.  ``element_type='tetra'`` cuts
+    every hex into six tetrahedra (Kuhn subdivision; faces are triangles, so jitter is
+    allowed)."""
     if prism_fraction > 0.0 and jitter > 0.0:
         raise ValueError("prism_fraction needs planar hex faces: use jitter = 0")
+    if element_type not in ("hex", "tetra"):
+        raise NotImplementedError("create_3D_grid builds hex, mixed hex/prism and tetra meshes")
     pts = _lattice(origin, nx, ny, nz, lx, ly, lz)
     if jitter > 0.0:
         pts = jitter_interior_nodes(pts, nx, ny, nz, (lx / nx, ly / ny, lz / nz), jitter, seed)
     conn = _hex_connectivity(nx, ny, nz)
+    if element_type == "tetra":
+        tets = _tets_of_hexes(conn, pts)
+        cells = np.hstack([np.full((tets.shape[0], 1), 4), tets]).ravel()
+        return UnstructuredGrid(cells, np.full(tets.shape[0], TETRA), pts)
     if prism_fraction > 0.0:
         split = np.random.default_rng(seed).random(conn.shape[0]) < prism_fraction
         cells, types = _cells_with_prisms(conn, split)
