@@ -110,9 +110,9 @@ typedef struct wcfd_krylov_ws {
     float*    vec;        /* wcfd_krylov_workspace_floats(C, ncomp) floats            */
     double*   partials;   /* 8 * WCFD_MAX_BLOCKS doubles (reduction partials)         */
     double*   results;    /* unused, may be NULL                                      */
-    uint32_t* barrier;    /* WCFD_BARRIER_WORDS words: per-block arrival flags, then the
-                             error word and the aggregator's release word; every
-                             solve call zeroes them first                            */
+    uint32_t* barrier;    /* WCFD_BARRIER_WORDS words: [WCFD_MAX_BLOCKS] the error word,
+                             [WCFD_MAX_BLOCKS + 2] the grid barrier's arrival counter
+                             (the rest unused); every solve call zeroes them first   */
 } wcfd_krylov_ws;
 
 typedef struct wcfd_solve_stats {
