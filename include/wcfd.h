@@ -263,8 +263,9 @@ int wcfd_cg(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws, doub
  * x64 (fp64, warm start in, result out; x32 receives its fp32 copy).  Each of `sweeps`
  * sweeps computes r = b - A x64 in fp64, solves A d = r with the fp32 CG (wcfd_cg's
  * kernels) down to ||r_d|| <= inner_rtol ||r|| or maxiter, and adds d to x64.  work holds
- * 2 C floats.  `stats` describes the last sweep's correction solve: its initial_residual is
- * ||b - A x64|| (fp32-rounded) before that sweep. */
+ * 2 C + 4 floats.  `stats` (device memory) describes the correction solves: iterations is
+ * their total over the sweeps, the other fields describe the last sweep's solve (its
+ * initial_residual is ||b - A x64||, fp32-rounded, before that sweep). */
 int wcfd_cg_refine(const wcfd_mesh* m, wcfd_system A, double* x64, float* x32, float* work, wcfd_krylov_ws ws,
                    int32_t sweeps, double inner_rtol, int32_t maxiter, wcfd_solve_stats* stats, void* stream);
 

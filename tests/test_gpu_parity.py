@@ -257,13 +257,15 @@ def test_cg_paths_agree_with_oracle(case):
     assert rel_l2(out[1][0], out[3][0]) < 3e-4
 
 
-def test_cylinder_piso_with_correction_tracks_oracle():
-    """The cylinder-in-channel PISO case, small: jittered all-hex O-grid around a cylinder, parabolic inlet,
-    PISO with 2 correctors and the non-orthogonal Laplacian correction."""
+@pytest.mark.parametrize("prisms", [False, True])
+def test_cylinder_piso_with_correction_tracks_oracle(prisms):
+    """The cylinder-in-channel PISO case, small: jittered O-grid of hexes around a cylinder and
+    a far field of hexes or of prisms (the prism/hex mesh of the benchmark case), parabolic
+    inlet, PISO with 2 correctors and the non-orthogonal Laplacian correction."""
     from warpcfd_gb300.preprocess import (Mesh, create_cylinder_channel_grid, define_boundary_walls,
                                           define_cylinder_group)
 
-    g, info = create_cylinder_channel_grid(scale=0.25, jitter=0.1, seed=5)
+    g, info = create_cylinder_channel_grid(scale=0.18 if prisms else 0.25, jitter=0.1, seed=5, prisms=prisms)
     m = Mesh(g)
     define_boundary_walls(m)
     define_cylinder_group(m, info["cylinder"])
@@ -326,13 +328,22 @@ def test_fp64_refined_pressure_solve_is_fp64_accurate():
     C = model.num_cells
     x64 = torch.zeros(C, dtype=torch.float64, device="cuda")
     x32 = torch.zeros(C, dtype=torch.float32, device="cuda")
-    work = torch.zeros(2 * C, dtype=torch.float32, device="cuda")
+    work = torch.zeros(2 * C + 4, dtype=torch.float32, device="cuda")
     st = torch.zeros(_lib.STATS_BYTES, dtype=torch.uint8, device="cuda")
     _lib.call("wcfd_cg_refine", ct.byref(model.mesh_struct()), pe.system_struct(), ct.c_void_p(x64.data_ptr()),
               ct.c_void_p(x32.data_ptr()), ct.c_void_p(work.data_ptr()), pe.workspace_struct(), 4, 1e-3, 500,
               ct.c_void_p(st.data_ptr()), ct.c_void_p(torch.cuda.current_stream().cuda_stream))
     torch.cuda.synchronize()
     err64 = rel_l2(x64.cpu().numpy(), x_exact)
+    it4 = int(np.frombuffer(st.cpu().numpy().tobytes(), dtype=_lib.STATS_DTYPE)[0]["iterations"])
+    # the statistics count the correction solves of every sweep: more than one sweep's
+    x1 = torch.zeros(C, dtype=torch.float64, device="cuda")
+    _lib.call("wcfd_cg_refine", ct.byref(model.mesh_struct()), pe.system_struct(), ct.c_void_p(x1.data_ptr()),
+              ct.c_void_p(x32.data_ptr()), ct.c_void_p(work.data_ptr()), pe.workspace_struct(), 1, 1e-3, 500,
+              ct.c_void_p(st.data_ptr()), ct.c_void_p(torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    it1 = int(np.frombuffer(st.cpu().numpy().tobytes(), dtype=_lib.STATS_DTYPE)[0]["iterations"])
+    assert it4 > it1 > 0, (it4, it1)
     # one fp32 CG to its floor, for comparison
     x_plain = torch.zeros(C, dtype=torch.float32, device="cuda")
     pe.tol, pe.max_iter = 0.0, 500

@@ -142,7 +142,7 @@ class IncompressibleSolver:
         ve, pe = self.vel_equation, self.p_corr_equation
         if self.p_refine > 0 and self.p_x64 is None:
             self.p_x64 = pe.x.to(torch.float64)
-            self.p_work = torch.zeros(2 * m.num_cells, dtype=torch.float32, device=m.device)
+            self.p_work = torch.zeros(2 * m.num_cells + 4, dtype=torch.float32, device=m.device)
         return _lib.Case_t(self._mesh_t, m.bc_struct(), m.state_struct(), ve.system_struct(), pe.system_struct(),
                            self.HbyA.data_ptr(), pe.x.data_ptr(), self.rUA.data_ptr(), self.rUA_faces.data_ptr(),
                            self.div_u.data_ptr(),

@@ -456,6 +456,9 @@ int wcfd_cg_refine(const wcfd_mesh* m, wcfd_system A, double* x64, float* x32, f
         if (rc) return rc;
         refine_update_kernel<<<gc, kBlock, 0, st>>>(C, x64, d, x32);
         LAUNCH_CHECK("refine_update_kernel");
+        refine_count_kernel<<<1, 1, 0, st>>>(stats, reinterpret_cast<int*>(work + 2 * (size_t)C), sw == 0,
+                                             sw == sweeps - 1);
+        LAUNCH_CHECK("refine_count_kernel");
     }
     return WCFD_OK;
 }

@@ -68,6 +68,7 @@ const void* cg1_cluster_kernel_for(int W, int R);
 size_t cluster_cg1_smem_bytes(int R, int W);
 const void* residual64_kernel_for(int W);
 __global__ void refine_update_kernel(int C, double* x64, const float* d, float* x32);
+__global__ void refine_count_kernel(wcfd_solve_stats* stats, int* acc, int first, int last);
 
 inline int grid_for(long long n, int bs = kBlock) { return (int)((n + bs - 1) / bs); }
 

@@ -438,6 +438,14 @@ __global__ void __launch_bounds__(kBlock) residual64_kernel(wcfd_mesh m, wcfd_sy
     r[i] = (float)((double)A.rhs[i] - acc);
 }
 
+// running total of the correction solves' iterations over the refinement sweeps; the last
+// sweep writes the total into its statistics
+__global__ void refine_count_kernel(wcfd_solve_stats* stats, int* acc, int first, int last) {
+    const int a = (first ? 0 : *acc) + stats->iterations;
+    *acc = a;
+    if (last) stats->iterations = a;
+}
+
 __global__ void __launch_bounds__(kBlock) refine_update_kernel(int C, double* __restrict__ x64,
                                                                const float* __restrict__ d, float* __restrict__ x32) {
     const int i = blockIdx.x * kBlock + threadIdx.x;

@@ -207,14 +207,17 @@ def _block(xy):
 
 
 def create_cylinder_channel_grid(scale=1.0, dz=0.01, jitter=0.1, seed=0, length=2.2, height=0.41,
-                                 center=(0.2, 0.2), diameter=0.1, box=0.1):
-    """All-hex 2D-extruded channel ``length`` x ``height`` around a cylinder (one cell thick).
+                                 center=(0.2, 0.2), diameter=0.1, box=0.1, prisms=False):
+    """2D-extruded channel ``length`` x ``height`` around a cylinder (one cell thick).
 
     Nine structured blocks: an O-grid of four quadrants between the cylinder (radius
     diameter/2) and a square of half-width ``box`` around it, and eight rectangular blocks
-    filling the rest of the channel, all with matching nodes.  ``scale`` = 1.0 gives about
-    96k cells, 1.625 about 254k.  Interior nodes (not on the walls, inlet, outlet or the
-    cylinder) move by up to ``jitter`` of their shortest incident edge, from ``seed``.
+    filling the rest of the channel, all with matching nodes.  All hex by default:
+    ``scale`` = 1.0 gives about 96k cells, 1.625 about 254k.  With ``prisms`` every quad
+    of the eight rectangular blocks is cut into two triangles, so the far field is prisms
+    (wedges) and the O-grid hexes: a prism/hex mesh (``scale`` = 1.15 gives about 245k
+    cells).  Interior nodes (not on the walls, inlet, outlet or the cylinder) move by up to
+    ``jitter`` of their shortest incident edge, from ``seed``.
 
     Returns (grid, info) with info['cylinder'] = (cx, cy, r) for grouping the cylinder faces.
     """
@@ -230,7 +233,7 @@ def create_cylinder_channel_grid(scale=1.0, dz=0.01, jitter=0.1, seed=0, length=
     nr = max(4, int(round(32 * scale)))
     xs = [np.linspace(0.0, x0, nA + 1), np.linspace(x0, x1, nB + 1), np.linspace(x1, length, nC + 1)]
     ys = [np.linspace(0.0, y0, na + 1), np.linspace(y0, y1, nB + 1), np.linspace(y1, height, nc + 1)]
-    pts_list, quads_list, off = [], [], 0
+    pts_list, quads_list, far_list, off = [], [], [], 0
     for bi in range(3):
         for bj in range(3):
             if bi == 1 and bj == 1:
@@ -239,6 +242,7 @@ def create_cylinder_channel_grid(scale=1.0, dz=0.01, jitter=0.1, seed=0, length=
             p, q = _block(np.stack([X, Y], axis=-1))
             pts_list.append(p)
             quads_list.append(q + off)
+            far_list.append(np.ones(len(q), dtype=bool))
             off += len(p)
     # O-grid: quadrant k spans angles [th0, th0 + 90deg]; the outer edge is a box side
     t = np.linspace(0.0, 1.0, nB + 1)
@@ -260,6 +264,7 @@ def create_cylinder_channel_grid(scale=1.0, dz=0.01, jitter=0.1, seed=0, length=
         p, q = _block(blk[:, ::-1, :])
         pts_list.append(p)
         quads_list.append(q + off)
+        far_list.append(np.zeros(len(q), dtype=bool))
         off += len(p)
     pts2, inv = _merge_nodes(np.concatenate(pts_list))
     quads = inv[np.concatenate(quads_list)]
@@ -286,6 +291,11 @@ def create_cylinder_channel_grid(scale=1.0, dz=0.01, jitter=0.1, seed=0, length=
     nn = len(pts2)
     pts3 = np.concatenate([np.column_stack([pts2, np.zeros(nn)]), np.column_stack([pts2, np.full(nn, dz)])])
     hexes = np.concatenate([quads, quads + nn], axis=1)
+    if prisms:
+        # counter-clockwise quads -> two counter-clockwise triangles -> two wedges in place
+        far = np.concatenate(far_list)
+        flat, types = _cells_with_prisms(hexes, far)
+        return UnstructuredGrid(flat, types, pts3), {"cylinder": (cx, cy, r0)}
     cells = np.hstack([np.full((len(hexes), 1), 8), hexes]).ravel()
     return UnstructuredGrid(cells, np.full(len(hexes), HEXAHEDRON), pts3), {"cylinder": (cx, cy, r0)}
 
