@@ -114,6 +114,12 @@ int launch_krylov(const void* fn, int slot, const wcfd_mesh* m, wcfd_system A, f
 
 int g_krylov_path = 0;  // 0 automatic, 1 grid-cooperative only, 2 cluster-resident when it fits, 3 as 2 with the single-reduction CG
 
+// rows per CTA below which the cluster CG takes the smallest cluster that holds the system
+// (larger systems take 16 CTAs); 2048 = two rows per thread of a 1,024-thread CTA
+#ifndef WCFD_CLUSTER_ROW_CAP
+#define WCFD_CLUSTER_ROW_CAP 2048
+#endif
+
 // Cluster-resident CG when the system fits in the shared memory of one cluster of up to
 // 16 CTAs; returns -1 (caller falls back to the grid-cooperative kernel) otherwise.
 int try_cluster_cg(const wcfd_mesh* m, wcfd_system A, float* x, double atol, int maxiter,
@@ -128,7 +134,7 @@ int try_cluster_cg(const wcfd_mesh* m, wcfd_system A, float* x, double atol, int
     int cs = 0, R = 0;
     for (int c = 1; c <= 16; c *= 2) {
         const long long r = (C + c - 1) / c;
-        if (r <= rmax && (r <= 2048 || c == 16)) {
+        if (r <= rmax && (r <= WCFD_CLUSTER_ROW_CAP || c == 16)) {
             cs = c;
             R = (int)r;
             break;
