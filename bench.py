@@ -261,6 +261,32 @@ def cpu_baseline(workload, mesh, seconds=15.0, warm=3):
                       f"fp32 restatement (oracle/simple_ref.py), single thread"}
 
 
+def fp64_field_error(workload, mesh, steps=20):
+    """Every field of a fresh GPU run (fp32, the drop-in path) against the fp64 oracle run
+    of the same method, both ``steps`` outer iterations from zero fields: relative L2
+    (u, v, w against ||U||, p against ||p||).  Part of the CPU leg: the oracle is the
+    checker here, not the thing measured."""
+    import torch
+
+    if workload not in ("channel", "cavity"):
+        return {"unavailable": f"the fp64 numpy oracle does not run {workload} within the bench's time"}
+    model, solver = build_gpu_case(workload, mesh)
+    for _ in range(steps):
+        solver.step()
+    torch.cuda.synchronize()
+    g = model.cell_values.double().cpu().numpy()
+    oc = build_oracle_case(workload, mesh, T=np.float64)
+    t0 = time.perf_counter()
+    oracle_step(oc, workload, steps)
+    o = np.asarray(oc.cell_values, dtype=np.float64)
+    un = max(float(np.linalg.norm(o[:, 0:3])), 1e-300)
+    pn = max(float(np.linalg.norm(o[:, 3])), 1e-300)
+    err = {f: float(np.linalg.norm(g[:, i] - o[:, i]) / un) for i, f in enumerate("uvw")}
+    err["p"] = float(np.linalg.norm(g[:, 3] - o[:, 3]) / pn)
+    return {"steps": steps, "rel_l2": err, "oracle": "fp64 numpy restatement of the same method",
+            "oracle_seconds": round(time.perf_counter() - t0, 2)}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -485,6 +511,7 @@ def run_ours(args):
         line["clocks"] = clocks.summary()
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(args.workload, mesh, seconds=args.cpu_seconds)
+            line["fp64_oracle"] = fp64_field_error(args.workload, mesh)
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()

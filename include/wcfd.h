@@ -164,7 +164,7 @@ typedef struct wcfd_case {
     float*         rua_faces;  /* [K]                                                */
     float*         div;        /* [C]   div of the mass flux                          */
     double*        p_x64;      /* [C]   fp64 pressure solution (p_refine > 0 only)       */
-    float*         p_work;     /* [2C]  refinement residual and correction (p_refine > 0) */
+    float*         p_work;     /* [2C+4] refinement residual, correction, sweep count (p_refine > 0) */
     wcfd_krylov_ws ws_u;       /* momentum workspace (ncomp 3)                        */
     wcfd_krylov_ws ws_p;       /* pressure workspace (ncomp 1)                        */
     wcfd_solve_stats* stats;   /* [2]: [0] momentum, [1] pressure (last corrector)    */
