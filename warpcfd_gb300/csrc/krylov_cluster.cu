@@ -267,7 +267,7 @@ __global__ void __launch_bounds__(CBS) cg_cluster_batched(const wcfd_case* __res
 // during the solve are read through L2 (ld.cg).  Same algorithm and arithmetic as
 // bicgstab_kernel (krylov.cu).
 template <int W>
-__global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case* __restrict__ cases, int cs_req) {
+__device__ __forceinline__ void bicgstab_cluster_body(const wcfd_case& cse) {
     __shared__ ff slots[2 * 3 * 16];
     __shared__ ff sbuf[2 * CBS];
     struct Scal {
@@ -276,7 +276,6 @@ __global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case*
         int go, status, k;
     };
     __shared__ Scal sc;
-    const wcfd_case& cse = cases[blockIdx.x / cs_req];
     const unsigned me = cluster_rank();
     const unsigned cs = cluster_nranks();
     const int C = cse.mesh.n_cells;
@@ -475,6 +474,11 @@ __global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case*
         cse.stats[0].status = st;
         cse.stats[0].residual = sqrt(ff_to_double(sc.rr));
     }
+}
+
+template <int W>
+__global__ void __launch_bounds__(CBS) bicgstab_cluster_batched(const wcfd_case* __restrict__ cases, int cs_req) {
+    bicgstab_cluster_body<W>(cases[blockIdx.x / cs_req]);
 }
 
 #define WCFD_W_SWITCH(NAME)                      \
