@@ -79,15 +79,34 @@ __device__ __forceinline__ void momentum_assemble_body(const wcfd_mesh& m, const
     float b[3] = {0.0f, 0.0f, 0.0f};
     int j = 0;
     const float4* slots = reinterpret_cast<const float4*>(m.cell_slot);
-    for (int f = 0; f < m.faces_per_cell; ++f) {
-        const int sk = __float_as_int(__ldg(&slots[(size_t)f * C + c].w));
+    // Every slot's face reference first, then every face's flux, neighbour and coefficient,
+    // all independent loads: a thread's chain of global-memory round trips is two deep
+    // instead of two per face (on small meshes this kernel is bound by that latency).
+    // Slots past faces_per_cell and null slots read face 0 and are skipped below.
+    int sks[kMaxSlots];
+#pragma unroll
+    for (int f = 0; f < kMaxSlots; ++f)
+        sks[f] = f < m.faces_per_cell ? __float_as_int(__ldg(&slots[(size_t)f * C + c].w)) : kNullSlot;
+    float mds[kMaxSlots], gds[kMaxSlots];
+    int nbs[kMaxSlots];
+#pragma unroll
+    for (int f = 0; f < kMaxSlots; ++f) {
+        const int sk = sks[f];
+        const int k = sk == kNullSlot ? 0 : sk >= 0 ? sk : ~sk;
+        mds[f] = s.mass_fluxes[k];
+        nbs[f] = __ldg(m.face_nbr + k);
+        gds[f] = __ldg(m.face_gdiff + k);
+    }
+#pragma unroll
+    for (int f = 0; f < kMaxSlots; ++f) {
+        const int sk = sks[f];
         if (sk == kNullSlot) continue;
         const bool owner_side = sk >= 0;
         const int k = owner_side ? sk : ~sk;
-        const float md = s.mass_fluxes[k];
-        const int N = __ldg(m.face_nbr + k);
+        const float md = mds[f];
+        const int N = nbs[f];
         if (N >= 0) {
-            const float dcoef = nu * __ldg(m.face_gdiff + k);
+            const float dcoef = nu * gds[f];
             float w0, w1;
             if (owner_side) {
                 w0 = md > 0.0f ? md : 0.0f;
@@ -205,12 +224,27 @@ __device__ __forceinline__ void pressure_assemble_body(const wcfd_mesh& m, const
     int j = 0;
     const bool ref = (c == prm.ref_cell);
     const float4* slots = reinterpret_cast<const float4*>(m.cell_slot);
-    for (int f = 0; f < m.faces_per_cell; ++f) {
-        const int sk = __float_as_int(__ldg(&slots[(size_t)f * C + c].w));
+    // the same two-deep load structure as the momentum assembly
+    int sks[kMaxSlots];
+#pragma unroll
+    for (int f = 0; f < kMaxSlots; ++f)
+        sks[f] = f < m.faces_per_cell ? __float_as_int(__ldg(&slots[(size_t)f * C + c].w)) : kNullSlot;
+    float cfs[kMaxSlots];
+    int nbs[kMaxSlots];
+#pragma unroll
+    for (int f = 0; f < kMaxSlots; ++f) {
+        const int sk = sks[f];
+        const int k = sk == kNullSlot ? 0 : sk >= 0 ? sk : ~sk;
+        nbs[f] = __ldg(m.face_nbr + k);
+        cfs[f] = rua_faces[k] * __ldg(m.face_gdiff + k);
+    }
+#pragma unroll
+    for (int f = 0; f < kMaxSlots; ++f) {
+        const int sk = sks[f];
         if (sk == kNullSlot) continue;
         const int k = sk >= 0 ? sk : ~sk;
-        const int N = __ldg(m.face_nbr + k);
-        const float coef = rua_faces[k] * __ldg(m.face_gdiff + k);
+        const int N = nbs[f];
+        const float coef = cfs[f];
         if (N >= 0) {
             d -= coef;
             sys.off[(size_t)j * C + c] = ref ? 0.0f : coef;
