@@ -125,10 +125,18 @@ __device__ __forceinline__ void gradient_body(const wcfd_mesh& m, const wcfd_sta
     for (int o = 0; o < 4; ++o) g[o][0] = g[o][1] = g[o][2] = 0.0f;
     float dv = 0.0f;
     const float4* slots = reinterpret_cast<const float4*>(m.cell_slot);
-    for (int f = 0; f < m.faces_per_cell; ++f) {
-        // a null slot (mixed meshes) reads face 0 and adds nothing: its vector is zero and
-        // its flux is masked; a select, not a branch, so the loads stay uniform
-        const float4 sl = __ldg(slots + (size_t)f * C + c);
+    // every slot record first (independent loads), then the faces: a thread's chain of
+    // global-memory round trips is two deep instead of two per face
+    float4 sls[kMaxSlots];
+#pragma unroll
+    for (int f = 0; f < kMaxSlots; ++f)
+        sls[f] = f < m.faces_per_cell ? __ldg(slots + (size_t)f * C + c)
+                                      : make_float4(0.0f, 0.0f, 0.0f, __int_as_float(kNullSlot));
+#pragma unroll
+    for (int f = 0; f < kMaxSlots; ++f) {
+        // a null slot (mixed meshes, or past faces_per_cell) reads face 0 and adds nothing:
+        // its vector is zero and its flux is masked; a select, not a branch
+        const float4 sl = sls[f];
         const int sk = __float_as_int(sl.w);
         const bool real = sk != kNullSlot;
         const int k = !real ? 0 : sk >= 0 ? sk : ~sk;
