@@ -8,6 +8,12 @@
 
 using namespace wcfd;
 
+// rows per block the grid-cooperative Krylov kernels are sized for (capped at the blocks
+// that can be co-resident)
+#ifndef WCFD_GRID_ROWS_PER_BLOCK
+#define WCFD_GRID_ROWS_PER_BLOCK 1024
+#endif
+
 namespace {
 
 thread_local char g_last_error[512] = "";
@@ -85,7 +91,7 @@ int launch_krylov(const void* fn, int slot, const wcfd_mesh* m, wcfd_system A, f
     const int cap = coop_capacity(fn, slot);
     LAUNCH_CHECK("occupancy query");
     RET_IF(cap <= 0, WCFD_ERR_CUDA, "solver kernel cannot be resident");
-    long long want = (m->n_cells + kSolverBlock - 1) / kSolverBlock;
+    long long want = (m->n_cells + WCFD_GRID_ROWS_PER_BLOCK - 1) / WCFD_GRID_ROWS_PER_BLOCK;
     int grid = (int)(want < cap ? want : cap);
     if (grid < 1) grid = 1;
     if (cudaMemsetAsync(ws.barrier, 0, WCFD_BARRIER_WORDS * sizeof(uint32_t), st) != cudaSuccess)
