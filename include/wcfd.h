@@ -148,7 +148,10 @@ typedef struct wcfd_params {
                                drops them): bit0 convection (skew correction), bit1 with
                                the upwindLinear term, bit2 the non-orthogonal diffusion
                                part (momentum and pressure); 0 = the reference          */
-    int32_t pad2_;
+    int32_t convection;     /* implicit convection weights of the momentum system: 0 upwind
+                               (incompressible.py:35; also upwindLinear, whose internal
+                               explicit part the reference drops), 1 central difference
+                               (convection.py:43-91 with interpolation 'central difference') */
 } wcfd_params;
 
 /* a full case: everything one SIMPLE iteration touches */

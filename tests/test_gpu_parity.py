@@ -638,3 +638,31 @@ def test_prism_and_mixed_meshes_track_oracle(case):
         assert rel_l2(g[:, 3], oc.cell_values[:, 3]) < tol_p, it
         st = solver.solve_stats()
         assert abs(st[1]["iterations"] - oc.log[-1][2]) <= 2
+
+
+@pytest.mark.parametrize("case", ["cavity_skew", "cavity3d"])
+def test_central_difference_convection_tracks_oracle(case):
+    """ConvectionTerm interpolation 'central difference' (convection.py:43-91): the fused
+    momentum assembly takes the (psi, 1 - psi) weights, as the oracle does; an unsupported
+    scheme raises instead of running upwind."""
+    mk = {"cavity_skew": (lambda: cavity_mesh(16, jitter=0.15, seed=11), cavity_bc, 0, 0.02),
+          "cavity3d": (lambda: cavity3d_mesh(8), cavity3d_bc, 0, 0.02)}[case]
+    model, solver, oc = make_pair(mk[0](), mk[1], ref_cell=mk[2], nu=mk[3])
+    solver.convection.interpolation = "central difference"
+    oc.conv_scheme = "central difference"
+    for it in range(4):
+        solver.step()
+        oracle_step(oc)
+        g = fields(model)
+        tol_u = 1e-5 if it == 0 else 1e-4
+        tol_p = 1e-4 if it == 0 else 1e-3
+        for o in range(3):
+            assert vel_err(g, oc.cell_values, o) < tol_u, (it, o)
+        assert rel_l2(g[:, 3], oc.cell_values[:, 3]) < tol_p, it
+    m2, s2, _ = make_pair(mk[0](), mk[1], ref_cell=mk[2], nu=mk[3])
+    for _ in range(4):
+        s2.step()
+    assert not torch.equal(model.cell_values, m2.cell_values)
+    solver.convection.interpolation = "custom"
+    with pytest.raises(NotImplementedError):
+        solver.step()

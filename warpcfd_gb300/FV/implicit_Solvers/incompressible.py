@@ -109,7 +109,15 @@ class IncompressibleSolver:
                              int(bool(m.skew_correction)), float(self.vel_equation.tol),
                              float(self.p_corr_equation.tol), int(self.p_refine), int(bool(self.rhie_chow)),
                              float(self.p_refine_rtol),
-                             float(self.vel_equation.rtol), float(self.p_corr_equation.rtol), self._explicit_bits())
+                             float(self.vel_equation.rtol), float(self.p_corr_equation.rtol), self._explicit_bits(),
+                             self._convection_code())
+
+    def _convection_code(self) -> int:
+        scheme = self.convection.interpolation
+        if scheme not in _lib.CONVECTION:
+            raise NotImplementedError(f"convection interpolation {scheme!r} is not available on this path "
+                                      "(upwind, upwindLinear, central difference)")
+        return _lib.CONVECTION[scheme]
 
     def _explicit_bits(self) -> int:
         if not self.explicit_internal_terms:
@@ -126,7 +134,7 @@ class IncompressibleSolver:
                 self.NUM_INNER_LOOPS, self.NUM_ORTHOGONAL_CORRECTORS, self.vel_equation.max_iter,
                 m.skew_correction, self.vel_equation.tol, self.p_corr_equation.tol, self._events_ptr,
                 self.p_refine, self.p_refine_rtol, self.vel_equation.rtol, self.p_corr_equation.rtol, self.rhie_chow,
-                self._explicit_bits())
+                self._explicit_bits(), self.convection.interpolation)
 
     def case_struct(self) -> _lib.Case_t:
         """The C struct of this case; rebuilt only when a parameter changed (the device

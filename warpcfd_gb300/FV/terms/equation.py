@@ -123,7 +123,8 @@ class Equation:
 
         * three velocity fields: ``[convection, -diffusion]`` (steady) or
           ``[ddt, convection, -diffusion]`` (transient) with ``explicit_terms =
-          -inv_density * grad_P``, upwind convection and a scalar viscosity set by calling
+          -inv_density * grad_P``, upwind (or upwindLinear, whose internal explicit part the
+          reference drops) or central-difference convection and a scalar viscosity set by calling
           the diffusion term (``diffusion(model, viscosity=nu)``) -> wcfd_assemble_momentum
           without relaxation (call ``relax`` next, as the reference does);
         * one field: a diffusion term of scale +1 with a scalar or per-face viscosity ->
@@ -158,10 +159,11 @@ class Equation:
             ex = [] if explicit_terms is None else (list(explicit_terms) if isinstance(explicit_terms, (list, tuple))
                                                     else [explicit_terms])
             grads = [t for t in ex if isinstance(t, GradTerm)]
-            if len(conv) != 1 or conv[0].interpolation != "upwind" or conv[0].scale != 1.0 or d.scale != -1.0 \
-                    or len(grads) != 1 or len(ex) != 1 or grads[0].scale >= 0.0 or (ddt and ddt[0].scale != 1.0):
-                raise NotImplementedError("the momentum system is [ddt,] upwind convection - diffusion with the "
-                                          "explicit source -(1/rho) grad p")
+            if len(conv) != 1 or conv[0].interpolation not in _lib.CONVECTION or conv[0].scale != 1.0 \
+                    or d.scale != -1.0 or len(grads) != 1 or len(ex) != 1 or grads[0].scale >= 0.0 \
+                    or (ddt and ddt[0].scale != 1.0):
+                raise NotImplementedError("the momentum system is [ddt,] convection (upwind, upwindLinear or "
+                                          "central difference) - diffusion with the explicit source -(1/rho) grad p")
             if torch.is_tensor(d.viscosity):
                 raise NotImplementedError("the momentum viscosity is a scalar")
             steady = not ddt
@@ -170,7 +172,7 @@ class Equation:
             rho = -1.0 / grads[0].scale
             prm = _lib.Params_t(float(d.viscosity), float(rho), 0.0, 0.0, float(ddt[0].dt) if ddt else 1.0, 0.0, -1,
                                 int(steady), 1, 1, self.max_iter, int(bool(fvm.skew_correction)), float(self.tol),
-                                float(self.tol), 0, 0, 1e-3, 0.0, 0.0)
+                                float(self.tol), 0, 0, 1e-3, 0.0, 0.0, 0, _lib.CONVECTION[conv[0].interpolation])
             case = _lib.Case_t(fvm.mesh_struct(d.correction), fvm.bc_struct(), fvm.state_struct(),
                                self.system_struct(), null, None, None, self._rua_scratch.data_ptr(), None, None,
                                None, None, _lib.KrylovWS_t(), _lib.KrylovWS_t(), None, prm, None)

@@ -23,6 +23,8 @@ STATUS_NAMES = {0: "ok", 1: "bad argument", 2: "cuda error", 3: "krylov breakdow
                 5: "barrier timeout", 6: "too large"}
 
 WCFD_U, WCFD_V, WCFD_W, WCFD_P, WCFD_ALL = 1, 2, 4, 8, 15
+# wcfd_params.convection per ConvectionTerm interpolation scheme
+CONVECTION = {"upwind": 0, "upwindLinear": 0, "central difference": 1}
 MAX_BLOCKS = 2048
 BARRIER_WORDS = MAX_BLOCKS + 4
 STATS_BYTES = 32
@@ -73,7 +75,7 @@ class Params_t(ct.Structure):
                 ("n_inner", ct.c_int32), ("n_ortho", ct.c_int32), ("maxiter", ct.c_int32), ("skew", ct.c_int32),
                 ("atol_u", ct.c_double), ("atol_p", ct.c_double), ("p_refine", ct.c_int32), ("rhie_chow", ct.c_int32),
                 ("p_refine_rtol", ct.c_double), ("rtol_u", ct.c_double), ("rtol_p", ct.c_double),
-                ("explicit_terms", ct.c_int32), ("pad2_", ct.c_int32)]
+                ("explicit_terms", ct.c_int32), ("convection", ct.c_int32)]
 
 
 class Case_t(ct.Structure):

@@ -13,6 +13,9 @@ namespace wcfd {
 //     internal face, this cell's side with outward flux F (= +mdot owner, -mdot neighbour):
 //       owner:     w_P = mdot if mdot > 0 else 0 ;  w_N = 0 if mdot > 0 else mdot
 //       neighbour: w_P = 0 if mdot > 0 else -mdot; w_N = -mdot if mdot > 0 else 0
+//     central difference (prm.convection = 1, interpolation 'central difference'):
+//       owner:     w_P = psi mdot ; w_N = (1 - psi) mdot
+//       neighbour: w_P = -(1 - psi) mdot ; w_N = -psi mdot
 //     boundary face: rhs -= mdot_b phi_b                                   (Q7)
 //   diffusion, scale -1 (diffusion.py:113-198): internal  w_P = -nu A/d, w_N = +nu A/d
 //     boundary fixed value:     diag += nu A/|r_Pf| ; rhs += nu A/|r_Pf| phi_b
@@ -108,7 +111,14 @@ __device__ __forceinline__ void momentum_assemble_body(const wcfd_mesh& m, const
         if (N >= 0) {
             const float dcoef = nu * gds[f];
             float w0, w1;
-            if (owner_side) {
+            if (prm.convection == 1) {
+                // central difference: (psi, 1 - psi) of mdot for the owner, the mirror image
+                // of -mdot for the neighbour (convection.py:43-91)
+                const float psi = __ldg(m.face_interp + 4 * (size_t)k + 3), psi2 = 1.0f - psi;
+                const float mn = -md;
+                w0 = owner_side ? psi * md : psi2 * mn;
+                w1 = owner_side ? psi2 * md : psi * mn;
+            } else if (owner_side) {
                 w0 = md > 0.0f ? md : 0.0f;
                 w1 = md > 0.0f ? 0.0f : md;
             } else {
