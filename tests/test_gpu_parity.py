@@ -666,3 +666,31 @@ def test_central_difference_convection_tracks_oracle(case):
     solver.convection.interpolation = "custom"
     with pytest.raises(NotImplementedError):
         solver.step()
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (2, 1), (3, 2), (33, 1), (7, 5)])
+def test_tiny_and_odd_meshes_track_oracle(shape):
+    """Edge cases of the mesh size: a single cell (every face a boundary face, no
+    off-diagonals: W = 0), one-row meshes (W = 1, 2), and sizes that fill no warp or block
+    evenly; the step follows the oracle.  The velocities of a one-cell-tall strip are ~4e-4,
+    so at the reference's absolute Krylov stop (1e-5) both runs stop anywhere within a few
+    percent of the solution; both solve to 1e-9 here, so the comparison measures the
+    arithmetic, not the stopping point."""
+    from warpcfd_gb300.preprocess import Mesh, create_2D_grid, define_boundary_walls
+
+    nx, ny = shape
+    m = Mesh(create_2D_grid((0, 0, 0), nx, ny, 1.0, 1.0, 0.1))
+    define_boundary_walls(m)
+    model, solver, oc = make_pair(m, cavity_bc, ref_cell=0, nu=0.05, atol=1e-9)
+    assert model._geo["ell_width"] == min(4, (nx > 1) * (1 + (nx > 2)) + (ny > 1) * (1 + (ny > 2)))
+    for it in range(3):
+        solver.step()
+        oracle_step(oc)
+        g = fields(model)
+        un = np.linalg.norm(oc.cell_values[:, 0:3])
+        if un > 0:
+            for o in range(3):
+                assert vel_err(g, oc.cell_values, o) < 1e-4, (it, o)
+        pn = np.linalg.norm(oc.cell_values[:, 3])
+        assert np.linalg.norm(g[:, 3] - oc.cell_values[:, 3]) <= 1e-3 * pn + 1e-6, it
+        assert np.isfinite(g).all()

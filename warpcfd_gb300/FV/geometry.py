@@ -91,7 +91,9 @@ def build_geometry(mesh, correction: bool = False) -> dict:
     nbr = cp.neighbors.astype(np.int64)
     m = nbr >= 0
     W = int(m.sum(axis=1).max()) if C else 0
-    ell_col = np.repeat(np.arange(C, dtype=np.int32)[None, :], max(W, 1), axis=0)[:W].copy()
+    # at least one row: a mesh without internal faces (W = 0, one cell) still hands the
+    # kernels a valid array, whose padding row they never read
+    ell_col = np.repeat(np.arange(C, dtype=np.int32)[None, :], max(W, 1), axis=0).copy()
     pos = (np.cumsum(m, axis=1) - 1)
     cc, ff = np.nonzero(m)
     ell_col[pos[cc, ff], cc] = nbr[cc, ff]

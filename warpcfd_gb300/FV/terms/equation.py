@@ -95,7 +95,7 @@ class Equation:
         """The system as a torch sparse CSR tensor (C*n x C*n), built on demand."""
         g = self.fvm._geo
         C, W, n = g["n_cells"], g["ell_width"], self.num_outputs
-        col = g["ell_col"].long()                       # (W, C)
+        col = g["ell_col"][:W].long()                   # (W, C)
         off = self.off[: W * C].reshape(W, C)
         own = torch.arange(C, device=col.device).expand(W, C)
         valid = col != own
