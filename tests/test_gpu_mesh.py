@@ -26,6 +26,8 @@ GRIDS = {
     "mixed3d": lambda: create_3D_grid((0, 0, 0), 8, 6, 5, 1.0, 1.0, 1.0, prism_fraction=0.4, seed=7),
     "tetra3d_jitter": lambda: create_3D_grid((0, 0, 0), 6, 5, 4, 1.0, 1.0, 1.0, element_type="tetra", jitter=0.2, seed=8),
     "cylinder": lambda: create_cylinder_channel_grid(scale=0.5)[0],
+    "single_hex": lambda: create_3D_grid((0, 0, 0), 1, 1, 1, 1.0, 1.0, 1.0),
+    "single_hex_as_tets": lambda: create_3D_grid((0, 0, 0), 1, 1, 1, 1.0, 1.0, 1.0, element_type="tetra"),
 }
 
 INT_FACE = ("unique_faces", "adjacent_cells", "cell_face_index", "is_boundary", "boundary_face_ids",
