@@ -357,7 +357,7 @@ def run_serve(args):
     if dist is not None:
         dist.barrier()
     with ClockSampler(local, enabled=not args.no_clocks) as clocks:
-        rep = Server(max_outer=args.max_outer).run(reqs)
+        rep = Server(max_outer=args.max_outer, max_active=args.max_active).run(reqs)
     summ = rep.summary()
     wall = max_over_ranks(summ["wall_s"])
     cell_its = sum_over_ranks(rep.cell_iterations)
@@ -542,7 +542,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=150.0)
     ap.add_argument("--no-clocks", action="store_true", help="do not sample nvidia-smi during the timed region")
-    ap.add_argument("--requests", type=int, default=256, help="serve workload: requests in the mix")
+    ap.add_argument("--requests", type=int, default=1024, help="serve workload: requests in the mix")
+    ap.add_argument("--max-active", type=int, default=256, help="serve workload: cases in flight at most")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve workload: Poisson arrival rate (1/s)")
     ap.add_argument("--max-outer", type=int, default=4000, help="serve workload: outer-iteration cap per request")
     ap.add_argument("--drop-in-sample", type=int, default=48, help="serve workload: requests run through the drop-in")
