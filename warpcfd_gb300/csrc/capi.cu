@@ -120,10 +120,12 @@ int launch_krylov(const void* fn, int slot, const wcfd_mesh* m, wcfd_system A, f
 
 int g_krylov_path = 0;  // 0 automatic, 1 grid-cooperative only, 2 cluster-resident when it fits, 3 as 2 with the single-reduction CG
 
-// rows per CTA below which the cluster CG takes the smallest cluster that holds the system
-// (larger systems take 16 CTAs); 2048 = two rows per thread of a 1,024-thread CTA
+// the cluster CG takes the smallest cluster whose CTAs hold at most this many rows each
+// (larger systems take 16 CTAs).  Its iteration is bound by the cluster reductions, so
+// more CTAs with fewer rows per thread are faster down to ~512 rows per CTA (measured on a
+// 4,096-row system: 2,048 rows per CTA 120 us per solve, 1,024 108, 512 106, 256 113)
 #ifndef WCFD_CLUSTER_ROW_CAP
-#define WCFD_CLUSTER_ROW_CAP 2048
+#define WCFD_CLUSTER_ROW_CAP 512
 #endif
 
 // Cluster-resident CG when the system fits in the shared memory of one cluster of up to
