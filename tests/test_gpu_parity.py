@@ -694,3 +694,19 @@ def test_tiny_and_odd_meshes_track_oracle(shape):
         pn = np.linalg.norm(oc.cell_values[:, 3])
         assert np.linalg.norm(g[:, 3] - oc.cell_values[:, 3]) <= 1e-3 * pn + 1e-6, it
         assert np.isfinite(g).all()
+
+
+@pytest.mark.parametrize("case", ["tet_cavity3d", "mixed_cavity3d"])
+def test_piso_on_tetra_and_mixed_meshes_tracks_oracle(case):
+    """Transient PISO (2 correctors, non-orthogonal correction) on a jittered tetrahedral
+    cavity and on a mixed hex/prism cavity follows the oracle."""
+    mk = {"tet_cavity3d": lambda: tet_cavity3d_mesh(5, jitter=0.1, seed=3),
+          "mixed_cavity3d": lambda: mixed_cavity3d_mesh(7, 0.5, seed=4)}[case]
+    model, solver, oc = make_pair(mk(), cavity3d_bc, steady=False, dt=0.01, inner=2, correction=True)
+    for it in range(4):
+        solver.step()
+        oracle_step(oc, None, None, steady=False, dt=0.01, inner=2)
+        g = fields(model)
+        for o in range(3):
+            assert vel_err(g, oc.cell_values, o) < 1e-4, (it, o)
+        assert rel_l2(g[:, 3], oc.cell_values[:, 3]) < 1e-3, it
