@@ -411,6 +411,14 @@ int wcfd_mesh_emit(const wcfd_mesh_cells* m, void* workspace, size_t workspace_b
 /* Message of the last failed mesh call on this thread. */
 const char* wcfd_mesh_last_error(void);
 
+/* Bounds and consistency check of a device geometry's index arrays (no reference
+ * counterpart; the stand-in for a sanitizer on the gathers): face owner / neighbour in
+ * range, boundary rows in range, every non-null cell slot naming a face that has the cell
+ * on that side, every off-diagonal column in range.  Each index is read only after the
+ * bounds it is used under were checked.  Synchronizes the stream; counts (host, 5 ints)
+ * receive the violations per kind; WCFD_ERR_ARGUMENT (and wcfd_mesh_last_error) if any. */
+int wcfd_check_mesh(const wcfd_mesh* m, int32_t* counts, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -94,16 +94,32 @@ class FVM:
         # the geometry is read-only on the device: models of the same mesh share one copy
         cache = self.mesh.__dict__.setdefault("_device_geometry", {})
         key = str(torch.device(dev))
-        if key not in cache:
+        fresh = key not in cache
+        if fresh:
             geo = build_geometry(self.mesh, correction=False)
             cache[key] = (geo, {k: (torch.from_numpy(np.ascontiguousarray(v)).to(dev) if isinstance(v, np.ndarray)
                                     else v) for k, v in geo.items()})
         self._geo_host, self._geo = cache[key]
+        if fresh:
+            self.check_mesh()
         self.boundary_type = torch.from_numpy(self.boundary.boundary_type.copy()).to(dev)
         self.boundary_value = torch.from_numpy(self.boundary.boundary_values.astype(np.float32)).to(dev)
         self.boundary_ids = self._geo["boundary_face"]
         self.init_global_arrays()
         self.finalized = True
+
+    def check_mesh(self):
+        """Bounds and consistency check of the device geometry's index arrays
+        (wcfd_check_mesh); raises WcfdError naming the violations.  Run once per mesh and
+        device by finalize()."""
+        import ctypes as ct
+        counts = (ct.c_int32 * 5)()
+        lib = _lib.load()
+        rc = lib.wcfd_check_mesh(ct.byref(self.mesh_struct()), counts,
+                                 ct.c_void_p(torch.cuda.current_stream(self.device).cuda_stream))
+        if rc != _lib.WCFD_OK:
+            raise _lib.WcfdError(rc, lib.wcfd_mesh_last_error().decode(errors="replace"))
+        return list(counts)
 
     def init_global_arrays(self):
         C, K, dev, T = self.num_cells, self.num_faces, self.device, self.float_dtype

@@ -145,6 +145,7 @@ _SIGS = {
     "wcfd_mesh_emit": (ct.c_int, [ct.POINTER(MeshCells_t), vp, ct.c_size_t, ct.POINTER(ct.c_int32),
                                   ct.POINTER(MeshFaces_t), vp]),
     "wcfd_mesh_last_error": (ct.c_char_p, []),
+    "wcfd_check_mesh": (ct.c_int, [ct.POINTER(Mesh_t), ct.POINTER(ct.c_int32), vp]),
     "wcfd_grid_barrier_check": (ct.c_int, [ct.c_int32, ct.c_int32, ct.POINTER(ct.c_int32), vp]),
 }
 

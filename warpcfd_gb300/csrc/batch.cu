@@ -158,6 +158,7 @@ extern "C" int wcfd_batch_simple_iteration(const wcfd_case* cases, int32_t n_cas
     const void* bi_fn = bicgstab_cluster_batched_for(d.ell_width);
     if (!cg_fn || !bi_fn) return WCFD_ERR_ARGUMENT;
     cudaStream_t st = S(stream);
+    NvtxRange step_range("wcfd batched iteration");
     const dim3 gf((d.max_faces + fb - 1) / fb, n_cases), gc((d.max_cells + fb - 1) / fb, n_cases);
     // incompressible.py:96-99
     face_pass_batched<<<gf, fb, 0, st>>>(cases, WCFD_ALL, 1u | 2u);

@@ -505,6 +505,7 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
     RET_IF(!c.hbya || !c.p_x || !c.rua || !c.rua_faces || !c.div || !c.stats, WCFD_ERR_ARGUMENT, "null case array");
     RET_IF(c.prm.n_inner < 0 || c.prm.n_ortho < 0, WCFD_ERR_ARGUMENT, "negative loop count");
     cudaStream_t st = S(stream);
+    NvtxRange step_range(c.prm.steady ? "wcfd SIMPLE iteration" : "wcfd PISO step");
     const wcfd_mesh& m = c.mesh;
     const uint32_t skew = c.prm.skew ? 4u : 0u;
     const int gf = grid_for(m.n_faces), gc = grid_for(m.n_cells);
@@ -521,7 +522,10 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
         if (c.events && c.events[i]) cudaEventRecord(reinterpret_cast<cudaEvent_t>(c.events[i]), st);
     };
     mark(0);
-    rc = bicgstab_solve(&m, c.mom, c.hbya, c.ws_u, c.prm.atol_u, c.prm.rtol_u, c.prm.maxiter, c.stats + 0, stream);
+    {
+        NvtxRange r("wcfd momentum solve");
+        rc = bicgstab_solve(&m, c.mom, c.hbya, c.ws_u, c.prm.atol_u, c.prm.rtol_u, c.prm.maxiter, c.stats + 0, stream);
+    }
     if (rc) return rc;
     mark(1);
     // :118-123
@@ -530,6 +534,7 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
     cell_to_face_kernel<<<gf, kBlock, 0, st>>>(m, c.rua, c.rua_faces);
     LAUNCH_CHECK("cell_to_face_kernel");
     for (int inner = 0; inner < c.prm.n_inner; ++inner) {
+        NvtxRange r("wcfd pressure corrector");
         for (int ortho = 0; ortho < c.prm.n_ortho; ++ortho) {
             // :127-132
             face_pass_kernel<<<gf, kBlock, 0, st>>>(m, c.bc, c.state, WCFD_ALL, 2u | skew, nullptr);

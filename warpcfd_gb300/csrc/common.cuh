@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 #include <climits>
 
@@ -278,5 +279,14 @@ __device__ bool grid_sync(const GridCtl& g, const ff* v, ff* out, unsigned phase
     __syncthreads();
     return true;
 }
+
+// NVTX range over a host scope (a stage of a step), for Nsight Systems timelines: one
+// cheap call each way when no tool is attached (NVTX v3, header-only)
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 }  // namespace wcfd

@@ -468,11 +468,92 @@ int exclusive_scan(int* a, long long n, int* sums, int* total, cudaStream_t st) 
 
 int blocks_for(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 
+// Validation of a device geometry (the index arrays every kernel gathers through): each
+// check reads an index only after the bounds it is used under have been checked, and each
+// violation adds one to a counter per kind.
+//   [0] face owner outside [0, C) or neighbour outside [-1, C) or equal to the owner
+//   [1] boundary row of a boundary face outside [0, B)
+//   [2] a cell slot that is not null and names a face outside [0, K)
+//   [3] a cell slot whose face does not have this cell on the side the slot says
+//   [4] an off-diagonal column outside [0, C)
+constexpr int kChecks = 5;
+
+__global__ void check_faces_kernel(wcfd_mesh m, int* __restrict__ bad) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= m.n_faces) return;
+    const int P = m.face_owner[k], N = m.face_nbr[k];
+    if (P < 0 || P >= m.n_cells || N < -1 || N >= m.n_cells || N == P) atomicAdd(bad + 0, 1);
+    if (N < 0) {
+        const int b = m.face_brow[k];
+        if (b < 0 || b >= m.n_bfaces) atomicAdd(bad + 1, 1);
+    }
+}
+
+__global__ void check_cells_kernel(wcfd_mesh m, int* __restrict__ bad) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= m.n_cells) return;
+    const float4* slots = reinterpret_cast<const float4*>(m.cell_slot);
+    for (int f = 0; f < m.faces_per_cell; ++f) {
+        const int sk = __float_as_int(slots[(size_t)f * m.n_cells + c].w);
+        if (sk == wcfd::kNullSlot) continue;
+        const int k = sk >= 0 ? sk : ~sk;
+        if (k < 0 || k >= m.n_faces) {
+            atomicAdd(bad + 2, 1);
+            continue;
+        }
+        if ((sk >= 0 ? m.face_owner[k] : m.face_nbr[k]) != c) atomicAdd(bad + 3, 1);
+    }
+    for (int j = 0; j < m.ell_width; ++j) {
+        const int col = m.ell_col[(size_t)j * m.n_cells + c];
+        if (col < 0 || col >= m.n_cells) atomicAdd(bad + 4, 1);
+    }
+}
+
 }  // namespace
 
 extern "C" {
 
 const char* wcfd_mesh_last_error(void) { return g_mesh_error; }
+
+int wcfd_check_mesh(const wcfd_mesh* m, int32_t* counts, void* stream) {
+    if (!m || !counts) return mesh_error(WCFD_ERR_ARGUMENT, "null mesh or counts");
+    if (m->n_cells <= 0 || m->n_faces <= 0 || m->faces_per_cell < 1 || m->faces_per_cell > wcfd::kMaxSlots ||
+        m->ell_width < 0 || m->ell_width > m->faces_per_cell)
+        return mesh_error(WCFD_ERR_ARGUMENT, "bad mesh sizes");
+    if (!m->face_owner || !m->face_nbr || !m->face_brow || !m->cell_slot || !m->ell_col)
+        return mesh_error(WCFD_ERR_ARGUMENT, "mesh has a null index array");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int* bad = nullptr;
+    if (cudaMalloc(&bad, kChecks * sizeof(int)) != cudaSuccess) MESH_CHECK("allocation");
+    int rc = WCFD_OK;
+    if (cudaMemsetAsync(bad, 0, kChecks * sizeof(int), st) != cudaSuccess) rc = WCFD_ERR_CUDA;
+    if (rc == WCFD_OK) {
+        check_faces_kernel<<<blocks_for(m->n_faces, 256), 256, 0, st>>>(*m, bad);
+        check_cells_kernel<<<blocks_for(m->n_cells, 256), 256, 0, st>>>(*m, bad);
+        int host[kChecks] = {0, 0, 0, 0, 0};
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpyAsync(host, bad, sizeof(host), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) {
+            rc = WCFD_ERR_CUDA;
+        } else {
+            int total = 0;
+            for (int i = 0; i < kChecks; ++i) {
+                counts[i] = host[i];
+                total += host[i];
+            }
+            if (total) {
+                std::snprintf(g_mesh_error, sizeof(g_mesh_error),
+                              "mesh index check: %d bad face ids, %d bad boundary rows, %d bad slot faces, "
+                              "%d slot/face mismatches, %d bad columns", host[0], host[1], host[2], host[3], host[4]);
+                rc = WCFD_ERR_ARGUMENT;
+            }
+        }
+    }
+    if (rc == WCFD_ERR_CUDA) std::snprintf(g_mesh_error, sizeof(g_mesh_error), "mesh index check: %s",
+                                           cudaGetErrorString(cudaGetLastError()));
+    cudaFree(bad);
+    return rc;
+}
 
 size_t wcfd_mesh_workspace_bytes(const wcfd_mesh_cells* m) {
     if (check_cells(m) != WCFD_OK) return 0;
