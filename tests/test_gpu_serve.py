@@ -35,3 +35,25 @@ def test_served_alone_equals_in_mix():
         got = by_id[req.rid]
         assert alone.iterations == got.iterations
         assert torch.equal(alone.fields.view(torch.int32), got.fields.view(torch.int32))  # bitwise, NaN too
+
+
+def test_server_rejects_what_it_can_never_serve():
+    """Requests no state of the server can admit -- too many cells for the largest bucket,
+    an unknown kind, Re = 0, more bytes than the whole HBM budget -- come back as
+    'rejected' while the rest are served; before, an over-budget head of the queue held
+    the admission loop for ever."""
+    from warpcfd_gb300.serve import Request, Server
+
+    reqs = [Request(0, "cavity", 32 * 32, 100.0, 1.0, 0.0), Request(1, "cavity", 70_000, 100.0, 1.0, 0.0),
+            Request(2, "bogus", 1024, 100.0, 1.0, 0.0), Request(3, "channel", 2048, 0.0, 1.0, 0.0),
+            Request(4, "cavity", 40 * 40, 200.0, 1.0, 0.0)]
+    rep = Server(max_outer=20, autotune=False).run(reqs)
+    st = {r.rid: r.status for r in rep.results}
+    assert len(st) == 5
+    assert st[1] == st[2] == st[3] == "rejected"
+    assert st[0] != "rejected" and st[4] != "rejected"
+    summary = rep.summary()
+    assert summary["rejected"] == 3 and summary["requests"] == 5
+    small = Server(hbm_budget=1 << 20, max_outer=20, autotune=False).run([Request(0, "cavity", 32 * 32, 100.0, 1.0, 0.0)])
+    assert [r.status for r in small.results] == ["rejected"]
+    assert "budget" in small.results[0].rejected

@@ -57,6 +57,7 @@ class Result:
     admitted: float
     finished: float
     fields: object = None
+    rejected: str = ""   # why the request was never admitted ("" when it was)
 
     @property
     def latency(self):
@@ -64,7 +65,11 @@ class Result:
 
     @property
     def status(self):
-        """converged, diverged (non-finite residual) or exhausted (max_outer reached)."""
+        """converged, diverged (non-finite residual), exhausted (max_outer reached) or
+        rejected (never admitted: too large for the batched solver or the HBM budget, or
+        a case that cannot be built)."""
+        if self.rejected:
+            return "rejected"
         if self.converged:
             return "converged"
         return "exhausted" if math.isfinite(self.residual) else "diverged"
@@ -204,7 +209,8 @@ class ServeReport:
     admit_s: float = 0.0
 
     def summary(self):
-        lat = np.array([r.latency for r in self.results]) if self.results else np.zeros(1)
+        served = [r for r in self.results if not r.rejected]
+        lat = np.array([r.latency for r in served]) if served else np.zeros(1)
         conv = [r for r in self.results if r.converged]
         lat_c = np.array([r.latency for r in conv]) if conv else np.full(1, np.nan)
         return {
@@ -212,6 +218,7 @@ class ServeReport:
             "converged": len(conv),
             "diverged": int(sum(r.status == "diverged" for r in self.results)),
             "exhausted": int(sum(r.status == "exhausted" for r in self.results)),
+            "rejected": int(sum(r.status == "rejected" for r in self.results)),
             "p50_converged_s": float(np.percentile(lat_c, 50)),
             "p99_converged_s": float(np.percentile(lat_c, 99)),
             "p50_s": float(np.percentile(lat, 50)),
@@ -271,6 +278,22 @@ class Server:
                 return i
         return len(self.bounds) - 1
 
+    def _never_admissible(self, req) -> str:
+        """Why ``req`` can never be admitted, or "": an unknown kind, a non-positive or
+        non-finite Re or speed, more cells than the largest bucket's cluster solver holds,
+        or more device bytes than the whole budget."""
+        if req.kind not in RELAXATION:
+            return f"unknown kind {req.kind!r}"
+        if not (math.isfinite(req.re) and req.re > 0 and math.isfinite(req.speed) and req.speed > 0):
+            return "Re and speed must be positive and finite"
+        if req.cells < 1:
+            return "no cells"
+        if req.cells > self.bounds[-1]:
+            return f"{req.cells} cells exceed the largest bucket ({self.bounds[-1]})"
+        if estimate_bytes(req.cells) + self._geometry_bytes > self.budget:  # geometry is never released
+            return f"needs about {estimate_bytes(req.cells)} device bytes, more than the budget ({self.budget})"
+        return ""
+
     def _admit(self, req, t0):
         """Build the case (the mesh and its device geometry come from caches) and charge its
         device bytes; a mesh's geometry is charged once, when it first reaches the device."""
@@ -310,12 +333,28 @@ class Server:
             # admission: arrived requests while slots and memory allow
             now = self.clock() - t0
             while qi < len(pending) and pending[qi].arrival <= now:
+                req = pending[qi]
+                # a request that no state of the server can admit is rejected, not queued
+                # (it would hold the head of the queue for ever)
+                why = self._never_admissible(req)
+                if why:
+                    report.results.append(Result(req.rid, req.kind, req.cells, 0, False, float("nan"), req.arrival,
+                                                 now, now, None, why))
+                    qi += 1
+                    continue
                 n_live = sum(len(a) for a in active) + sum(len(a) for a in incoming)
-                if n_live >= self.max_active or (used + self._geometry_bytes + estimate_bytes(pending[qi].cells)
+                if n_live >= self.max_active or (used + self._geometry_bytes + estimate_bytes(req.cells)
                                                  > self.budget):
                     break
                 ta = self.clock()
-                slot = self._admit(pending[qi], t0)
+                try:
+                    slot = self._admit(req, t0)
+                except (ValueError, KeyError, AssertionError, NotImplementedError, _lib.WcfdError) as e:
+                    report.admit_s += self.clock() - ta
+                    report.results.append(Result(req.rid, req.kind, req.cells, 0, False, float("nan"), req.arrival,
+                                                 now, self.clock() - t0, None, f"cannot build the case: {e}"))
+                    qi += 1
+                    continue
                 report.admit_s += self.clock() - ta
                 used += slot.bytes
                 report.peak_bytes = max(report.peak_bytes, used + self._geometry_bytes)
