@@ -26,11 +26,15 @@ __device__ __forceinline__ void face_pass_body(const wcfd_mesh& m, const wcfd_bc
                                                const float* __restrict__ rua_f = nullptr) {
     const int P = __ldg(m.face_owner + k);
     const int N = __ldg(m.face_nbr + k);
+    // the face's own records ([K] arrays) do not depend on the cell ids: issued with them,
+    // so a face is two global-memory round trips deep (ids and records, then the cells)
+    const float4 gi = __ldg(reinterpret_cast<const float4*>(m.face_interp) + k);
+    const float4 nrm = (flags & 2u) ? __ldg(reinterpret_cast<const float4*>(m.face_normal) + k)
+                                    : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     // an internal face with every field selected overwrites all four values: no read
     float4 fv = (N >= 0 && mask == WCFD_ALL) ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : ld4(s.face_values + 4 * (size_t)k);
     const float4 cp = ld4(s.cell_values + 4 * (size_t)P);
     if (N >= 0) {
-        const float4 gi = __ldg(reinterpret_cast<const float4*>(m.face_interp) + k);
         const float psi = gi.w;
         const float psi2 = 1.0f - psi;
         const float4 cn = ld4(s.cell_values + 4 * (size_t)N);
@@ -89,10 +93,9 @@ __device__ __forceinline__ void face_pass_body(const wcfd_mesh& m, const wcfd_bc
     }
     st4(s.face_values + 4 * (size_t)k, fv);
     if (flags & 2u) {
-        const float4 n = __ldg(reinterpret_cast<const float4*>(m.face_normal) + k);
+        const float4 n = nrm;
         float md = (fv.x * n.x + fv.y * n.y + fv.z * n.z) * n.w;
         if ((flags & 16u) && rua_f && N >= 0) {
-            const float4 gi = __ldg(reinterpret_cast<const float4*>(m.face_interp) + k);
             const float psi = gi.w, psi2 = 1.0f - psi;
             const float4 cn = ld4(s.cell_values + 4 * (size_t)N);
             const float* gP = s.cell_gradients + 12 * (size_t)P + 9;
