@@ -108,7 +108,7 @@ typedef struct wcfd_system {
 /* Krylov workspace (caller-allocated, see wcfd_krylov_workspace_floats) */
 typedef struct wcfd_krylov_ws {
     float*    vec;        /* wcfd_krylov_workspace_floats(C, ncomp) floats            */
-    double*   partials;   /* 8 * WCFD_MAX_BLOCKS doubles (reduction partials)         */
+    double*   partials;   /* 8 * WCFD_MAX_BLOCKS doubles (reduction partials), 16-byte aligned */
     double*   results;    /* unused, may be NULL                                      */
     uint32_t* barrier;    /* WCFD_BARRIER_WORDS words: [WCFD_MAX_BLOCKS] the error word,
                              [WCFD_MAX_BLOCKS + 2] the grid barrier's arrival counter

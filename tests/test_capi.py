@@ -76,3 +76,29 @@ def test_missing_library_fails_loudly(tmp_path):
 
     with pytest.raises(ImportError):
         _lib.load(tmp_path / "nope.so")
+
+
+def test_misaligned_krylov_partials_are_refused(built_lib):
+    """wcfd_cg refuses a partial-sum buffer that is not 16-byte aligned (the grid barrier
+    stores each block's sums there as one float4) before any device call: path 1 (grid
+    solver only) skips the cluster set-up, and the pointers below are only checked, never
+    dereferenced."""
+    from warpcfd_gb300 import _lib
+
+    lib = _lib.load()
+    buf = (ct.c_double * 64)()
+    base = (ct.addressof(buf) + 15) // 16 * 16
+    m = _lib.Mesh_t()
+    m.n_cells, m.n_faces, m.faces_per_cell, m.ell_width = 10, 20, 4, 4
+    for name, typ in _lib.Mesh_t._fields_:
+        if typ is ct.c_void_p:
+            setattr(m, name, base)
+    A = _lib.System_t(base, base, base, 1, 0)
+    ws = _lib.KrylovWS_t(base, base + 8, None, base)
+    assert lib.wcfd_set_krylov_path(1) == 0
+    try:
+        rc = lib.wcfd_cg(ct.byref(m), A, ct.c_void_p(base), ws, 1e-6, 10, ct.c_void_p(base), ct.c_void_p(None))
+    finally:
+        lib.wcfd_set_krylov_path(0)
+    assert rc == _lib.WCFD_ERR_ARGUMENT
+    assert b"16-byte" in lib.wcfd_last_error()

@@ -87,6 +87,9 @@ int launch_krylov(const void* fn, int slot, const wcfd_mesh* m, wcfd_system A, f
     RET_IF(!fn, WCFD_ERR_ARGUMENT, "no solver kernel for this off-diagonal width");
     RET_IF(!A.diag || !A.off || !A.rhs || !x || !ws.vec || !ws.partials || !ws.barrier || !stats,
            WCFD_ERR_ARGUMENT, "null solver argument");
+    // the grid barrier stores each block's partial sums as one float4
+    RET_IF(reinterpret_cast<uintptr_t>(ws.partials) % 16 != 0, WCFD_ERR_ARGUMENT,
+           "Krylov workspace: partials must be 16-byte aligned");
     RET_IF(maxiter < 0 || !(atol >= 0.0), WCFD_ERR_ARGUMENT, "bad atol or maxiter");
     const int cap = coop_capacity(fn, slot);
     LAUNCH_CHECK("occupancy query");
