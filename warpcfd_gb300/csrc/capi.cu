@@ -304,7 +304,10 @@ int wcfd_face_pass_flags(const wcfd_mesh* m, wcfd_bc bc, wcfd_state s, uint32_t 
     RET_IF(!bc.type || !bc.value || !s.cell_values || !s.cell_gradients || !s.face_values || !s.face_gradients ||
                !s.mass_fluxes,
            WCFD_ERR_ARGUMENT, "null field");
-    face_pass_kernel<<<grid_for(m->n_faces), kBlock, 0, S(stream)>>>(*m, bc, s, mask, flags & 15u, nullptr);
+    if (mask == WCFD_ALL)
+        face_pass_kernel<<<grid_for(m->n_faces), kBlock, 0, S(stream)>>>(*m, bc, s, mask, flags & 15u, nullptr);
+    else
+        face_pass_partial_kernel<<<grid_for(m->n_faces), kBlock, 0, S(stream)>>>(*m, bc, s, mask, flags & 15u, nullptr);
     LAUNCH_CHECK("face_pass_kernel");
     return WCFD_OK;
 }
@@ -561,8 +564,8 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
                                                    c.prm.steady ? c.prm.p_relax : 0.0f);
             LAUNCH_CHECK("p_update_kernel");
             // :150-156
-            face_pass_kernel<<<gf, kBlock, 0, st>>>(m, c.bc, c.state, WCFD_P, skew, nullptr);
-            LAUNCH_CHECK("face_pass_kernel");
+            face_pass_partial_kernel<<<gf, kBlock, 0, st>>>(m, c.bc, c.state, WCFD_P, skew, nullptr);
+            LAUNCH_CHECK("face_pass_partial_kernel");
             gradient_kernel<<<gc, kBlock, 0, st>>>(m, c.state, WCFD_P, nullptr, CorrectArgs{c.hbya, c.rua});
             LAUNCH_CHECK("gradient_kernel");
         }

@@ -12,6 +12,8 @@ struct CorrectArgs {
 
 __global__ void face_pass_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s, uint32_t mask, uint32_t flags,
                                  const float* rua_f);
+__global__ void face_pass_partial_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s, uint32_t mask, uint32_t flags,
+                                 const float* rua_f);
 __global__ void gradient_kernel(wcfd_mesh m, wcfd_state s, uint32_t mask, float* div, CorrectArgs corr);
 __global__ void mass_flux_kernel(wcfd_mesh m, wcfd_state s);
 __global__ void div_kernel(wcfd_mesh m, const float* mdot, float* div);

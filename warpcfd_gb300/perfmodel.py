@@ -52,6 +52,12 @@ def face_pass_bytes(C: int, K: int, Ki: int, B: int, mdot: bool = True) -> int:
     return b
 
 
+def face_pass_partial_bytes(C: int, K: int, Ki: int, B: int) -> int:
+    """One field (the pressure-only pass, no mass flux): face records read and written
+    whole (32), the cells' value records (16) and the field's 3 gradient components (12)."""
+    return 8 * K + 16 * Ki + 32 * K + 28 * C + B * (4 + 4 + 16 + 16 + 4)
+
+
 def gradient_bytes(C: int, K: int, F: int, div: bool = False) -> int:
     b = 16 * F * C + 16 * K + 48 * C
     if div:
