@@ -191,8 +191,8 @@ extern "C" int wcfd_batch_simple_iteration(const wcfd_case* cases, int32_t n_cas
             if (rc) return rc;
             p_update_batched<<<gc, fb, 0, st>>>(cases);
             BCHECK("p_update_batched");
-            face_pass_batched<<<gf, fb, 0, st>>>(cases, WCFD_P, 0u);
-            BCHECK("face_pass_batched");
+            face_pass_partial_batched<<<gf, fb, 0, st>>>(cases, WCFD_P, 0u);
+            BCHECK("face_pass_partial_batched");
             gradient_batched<<<gc, fb, 0, st>>>(cases, WCFD_P, 2);
             BCHECK("gradient_batched");
         }

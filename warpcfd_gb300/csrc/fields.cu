@@ -325,6 +325,17 @@ __global__ void __launch_bounds__(kMaxFieldBlock) face_pass_batched(const wcfd_c
     face_pass_body(c.mesh, c.bc, c.state, mask, flags | rc | (c.prm.skew ? 4u : 0u), k, c.rua_faces);
 }
 
+// the batched pass for a mask other than WCFD_ALL (the pressure-only pass), compiled
+// without the whole-record path like face_pass_partial_kernel
+__global__ void __launch_bounds__(kMaxFieldBlock, 3) face_pass_partial_batched(const wcfd_case* __restrict__ cases,
+                                                                              uint32_t mask, uint32_t flags) {
+    const wcfd_case& c = cases[blockIdx.y];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= c.mesh.n_faces) return;
+    const uint32_t rc = (c.prm.rhie_chow && (flags & 1u)) ? 16u : 0u;
+    face_pass_body<0>(c.mesh, c.bc, c.state, mask, flags | rc | (c.prm.skew ? 4u : 0u), k, c.rua_faces);
+}
+
 // mode 0: gradients only; 1: + divergence into case.div; 2: + velocity correction
 __global__ void __launch_bounds__(kMaxFieldBlock) gradient_batched(const wcfd_case* __restrict__ cases, uint32_t mask,
                                                            int mode) {

@@ -31,6 +31,7 @@ void launch_pressure_assemble(bool xt, int grid, cudaStream_t st, const wcfd_mes
 
 // batched forms over a device case table (blockIdx.y = case)
 __global__ void face_pass_batched(const wcfd_case* cases, uint32_t mask, uint32_t flags);
+__global__ void face_pass_partial_batched(const wcfd_case* cases, uint32_t mask, uint32_t flags);
 __global__ void gradient_batched(const wcfd_case* cases, uint32_t mask, int mode);
 __global__ void hbya_batched(const wcfd_case* cases);
 __global__ void rua_faces_batched(const wcfd_case* cases);
