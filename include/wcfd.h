@@ -295,9 +295,12 @@ int wcfd_krylov_solve(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_w
  * memory budgeted at start-up, plugins that may not allocate): the Krylov workspace is a
  * fixed array inside the library, sized for at most WCFD_NOALLOC_MAX_CELLS rows (about
  * 3.1 MiB, held by every GPU that loads the library until exit); larger systems return
- * WCFD_ERR_TOO_LARGE.  The first call on a device looks up the array's device address
- * (make it before any stream capture).  The call allocates nothing.  All calls share the
- * array, so calls that overlap on the GPU race; results are those of wcfd_cg. */
+ * WCFD_ERR_TOO_LARGE.  A call made outside stream capture looks the array's device
+ * address up (again, so a device reset is picked up); a call on a stream being captured
+ * uses the address remembered from the last uncaptured call on that device, so the first
+ * call on a device, and the first after a device reset, must come before any capture.
+ * The call allocates nothing.  All calls share the array, so calls that overlap on the
+ * GPU race; results are those of wcfd_cg. */
 #define WCFD_NOALLOC_MAX_CELLS 131072
 int wcfd_cg_noalloc(const wcfd_mesh* m, wcfd_system A, float* x, double atol, int32_t maxiter,
                     wcfd_solve_stats* stats, void* stream);

@@ -583,13 +583,17 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
 // workspace: a host code that drives the pressure solve through this C ABI with a
 // device-memory budget fixed at start-up, or a plugin that is not allowed to allocate
 // once its host application runs.  The array is a file-scope __device__ variable, so
-// every GPU that loads the library holds it (about 2.6 MiB) until the process exits.
+// every GPU that loads the library holds it (kNoAllocBytes, about 3.1 MiB) until the
+// process exits.
 //
 // The host only knows a stand-in for the array's name; its device address is looked up
-// with cudaGetSymbolAddress once per device (on the first call made with that device
-// current) and then passed to the kernel.  Make that first call before any stream
-// capture.  All calls share the one array: the call zeroes the barrier words it needs,
-// and calls that overlap on the GPU (other streams, other threads) race on it.
+// with cudaGetSymbolAddress and then passed to the kernel.  A call made outside stream
+// capture looks the address up again (so a device reset, which reloads the module at a
+// new address, is picked up) and remembers it per device; a call made while its stream
+// is being captured uses the remembered address, so the first call on a device, and the
+// first call after a device reset, must come before any capture.  All calls share the
+// one array: the call zeroes the barrier words it needs, and calls that overlap on the
+// GPU (other streams, other threads) race on it.
 namespace {
 
 constexpr size_t kNoAllocVecBytes = 6ull * WCFD_NOALLOC_MAX_CELLS * sizeof(float);
@@ -617,10 +621,20 @@ extern "C" int wcfd_cg_noalloc(const wcfd_mesh* m, wcfd_system A, float* x, doub
         cudaGetLastError();
         return set_error(WCFD_ERR_CUDA, "wcfd_cg_noalloc: no usable current device");
     }
+    // a failed query (e.g. the legacy stream while another stream captures in global
+    // mode) counts as capturing: only the remembered address is used then
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(S(stream), &cap) != cudaSuccess) {
+        cudaGetLastError();
+        cap = cudaStreamCaptureStatusActive;
+    }
+    const bool capturing = cap != cudaStreamCaptureStatusNone;
     void* base = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_addr[dev]) {
+        if (!capturing || !g_noalloc_addr[dev]) {
+            RET_IF(capturing, WCFD_ERR_ARGUMENT,
+                   "wcfd_cg_noalloc: the first call on a device must come before any stream capture");
             void* p = nullptr;
             const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
             if (e != cudaSuccess || !p) {
