@@ -7,7 +7,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-REFERENCE = "/root/reference"
+# the warp_cfd sources, read by CPU tests that check fixtures against them when present
+REFERENCE = os.environ.get("WCFD_REFERENCE", "/root/reference")
 
 
 def pytest_configure(config):

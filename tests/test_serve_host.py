@@ -5,7 +5,7 @@ import math
 import numpy as np
 
 from warpcfd_gb300.serve import (CHANNEL_ASPECT, RELAXATION, MeshCache, Request, Result, Server, ServeReport,
-                                 estimate_bytes, make_request_mix, side_ladder)
+                                 estimate_bytes, estimate_geometry_bytes, make_request_mix, side_ladder)
 
 
 def test_request_mix_is_seeded_and_within_bounds():
@@ -54,10 +54,7 @@ def test_never_admissible_names_the_reason():
     """The check that keeps the admission loop from waiting for ever on a request that no
     state of the server can hold.  Only the bounds, budget and charged geometry bytes are
     read, so the server's device state (streams) is not built here."""
-    srv = Server.__new__(Server)
-    srv.bounds = (4096, 16384, 65536)
-    srv.budget = 1 << 30
-    srv._geometry_bytes = 0
+    srv = _host_server((4096, 16384, 65536), 1 << 30)
     ok = Request(0, "cavity", 4096, 100.0, 1.0, 0.0)
     assert srv._never_admissible(ok) == ""
     assert "largest bucket" in srv._never_admissible(Request(1, "cavity", 70_000, 100.0, 1.0, 0.0))
@@ -65,6 +62,7 @@ def test_never_admissible_names_the_reason():
     assert "positive" in srv._never_admissible(Request(3, "channel", 1024, 0.0, 1.0, 0.0))
     assert "positive" in srv._never_admissible(Request(4, "channel", 1024, 100.0, math.nan, 0.0))
     assert "no cells" in srv._never_admissible(Request(5, "cavity", 0, 100.0, 1.0, 0.0))
+    srv._geometry_charged.add(srv._mesh_key(ok))      # its mesh is on the device already
     srv.budget = estimate_bytes(4096) - 1
     assert "budget" in srv._never_admissible(ok)
     # geometry already on the device is never released, so it counts against the budget
@@ -72,6 +70,55 @@ def test_never_admissible_names_the_reason():
     assert "budget" in srv._never_admissible(ok)
     srv._geometry_bytes = 10
     assert srv._never_admissible(ok) == ""
+
+
+def _host_server(bounds, budget):
+    """A Server with only the state its admission checks read (no device state)."""
+    srv = Server.__new__(Server)
+    srv.bounds = bounds
+    srv.budget = budget
+    srv.meshes = MeshCache()
+    srv._geometry_charged = set()
+    srv._geometry_bytes = 0
+    return srv
+
+
+def test_new_mesh_geometry_counts_against_the_budget():
+    """A request whose mesh is not on the device yet must fit together with that mesh's
+    geometry: the case alone would fit, the case plus its new geometry does not."""
+    req = Request(0, "channel", 16384, 200.0, 1.0, 0.0)
+    nx, ny = MeshCache().shape("channel", 16384)
+    geo = estimate_geometry_bytes(nx * ny)
+    assert geo > 0.3 * estimate_bytes(16384)
+    srv = _host_server((4096, 16384, 65536), estimate_bytes(16384) + geo - 1)
+    assert srv._new_geometry_bytes(req) == geo
+    assert not srv._fits(req, 0)
+    assert "budget" in srv._never_admissible(req)
+    # one more byte and it fits, with nothing else admitted
+    srv.budget += 1
+    assert srv._fits(req, 0) and srv._never_admissible(req) == ""
+    assert not srv._fits(req, 1)
+    # once that mesh's geometry is charged (on the device), only its measured bytes count
+    srv._geometry_charged.add(srv._mesh_key(req))
+    srv._geometry_bytes = geo // 2
+    assert srv._new_geometry_bytes(req) == 0
+    assert srv._fits(req, geo // 2)
+    # a request of another size has its own mesh and pays for its geometry again
+    other = Request(1, "channel", 8000, 200.0, 1.0, 0.0)
+    assert srv._new_geometry_bytes(other) > 0
+
+
+def test_geometry_estimate_bounds_the_built_geometry():
+    """estimate_geometry_bytes stays above the host-built geometry arrays the device
+    copies, on cavity and channel meshes of the mix."""
+    from warpcfd_gb300.FV.geometry import build_geometry
+
+    mc = MeshCache()
+    for kind, cells in (("cavity", 1024), ("channel", 6000), ("cavity", 20000)):
+        m = mc.get(kind, cells)
+        nb = sum(v.nbytes for v in build_geometry(m).values() if isinstance(v, np.ndarray))
+        C = m.cell_properties.faces.shape[0]
+        assert nb <= estimate_geometry_bytes(C) < 1.3 * nb
 
 
 def test_rejected_results_are_counted_and_kept_out_of_latency():

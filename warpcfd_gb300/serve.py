@@ -188,6 +188,14 @@ def estimate_bytes(cells: int) -> int:
     return int(1100 * cells + 2 * 8 * 2048 * 8 + 64 * 1024)
 
 
+def estimate_geometry_bytes(cells: int) -> int:
+    """Admission estimate of a mesh's device geometry before it is built: a 2D-extruded hex
+    mesh has about four faces per cell (68 B of face records each), six 16-byte cell slots
+    and four 4-byte off-diagonal columns per cell, about 390 B per cell; 420 B per cell plus
+    64 KiB stays above geometry_bytes() on the mix's meshes."""
+    return int(420 * cells + 64 * 1024)
+
+
 @dataclass
 class _Slot:
     req: Request
@@ -290,9 +298,29 @@ class Server:
             return "no cells"
         if req.cells > self.bounds[-1]:
             return f"{req.cells} cells exceed the largest bucket ({self.bounds[-1]})"
-        if estimate_bytes(req.cells) + self._geometry_bytes > self.budget:  # geometry is never released
-            return f"needs about {estimate_bytes(req.cells)} device bytes, more than the budget ({self.budget})"
+        # geometry on the device is never released: the case must fit beside all of it,
+        # and beside its own mesh's geometry when that is not on the device yet
+        need = estimate_bytes(req.cells) + self._new_geometry_bytes(req)
+        if need + self._geometry_bytes > self.budget:
+            return f"needs about {need} device bytes, more than the budget ({self.budget}) leaves"
         return ""
+
+    def _mesh_key(self, req):
+        return (req.kind,) + self.meshes.shape(req.kind, req.cells)
+
+    def _new_geometry_bytes(self, req) -> int:
+        """Estimated device bytes of ``req``'s mesh geometry if it is not on the device yet,
+        else 0 (it is then already charged)."""
+        key = self._mesh_key(req)
+        if key in self._geometry_charged:
+            return 0
+        return estimate_geometry_bytes(key[1] * key[2])
+
+    def _fits(self, req, used) -> bool:
+        """Whether ``req`` fits the budget now, beside the admitted cases' ``used`` bytes,
+        the geometry on the device and its own mesh's geometry if that is new."""
+        return (used + self._geometry_bytes + self._new_geometry_bytes(req) + estimate_bytes(req.cells)
+                <= self.budget)
 
     def _admit(self, req, t0):
         """Build the case (the mesh and its device geometry come from caches) and charge its
@@ -300,8 +328,9 @@ class Server:
         mesh = self.meshes.get(req.kind, req.cells)
         model, solver = build_solver(req, mesh, atol=self.atol, device=self.device, rtol=self.rtol)
         nb = case_bytes(model, solver, include_geometry=False)
-        if id(mesh) not in self._geometry_charged:
-            self._geometry_charged.add(id(mesh))
+        key = self._mesh_key(req)
+        if key not in self._geometry_charged:
+            self._geometry_charged.add(key)
             self._geometry_bytes += geometry_bytes(model)
         return _Slot(req, model, solver, nb, self.clock() - t0)
 
@@ -343,8 +372,7 @@ class Server:
                     qi += 1
                     continue
                 n_live = sum(len(a) for a in active) + sum(len(a) for a in incoming)
-                if n_live >= self.max_active or (used + self._geometry_bytes + estimate_bytes(req.cells)
-                                                 > self.budget):
+                if n_live >= self.max_active or not self._fits(req, used):
                     break
                 ta = self.clock()
                 try:
@@ -356,6 +384,18 @@ class Server:
                     qi += 1
                     continue
                 report.admit_s += self.clock() - ta
+                if used + slot.bytes + self._geometry_bytes > self.budget:
+                    # the measured bytes (or the mesh's measured geometry) exceed the
+                    # estimates: release the case; with nothing else admitted it can never
+                    # fit, otherwise it waits for cases to retire
+                    del slot
+                    if n_live == 0:
+                        report.results.append(Result(req.rid, req.kind, req.cells, 0, False, float("nan"),
+                                                     req.arrival, now, self.clock() - t0, None,
+                                                     "measured device bytes exceed the budget"))
+                        qi += 1
+                        continue
+                    break
                 used += slot.bytes
                 report.peak_bytes = max(report.peak_bytes, used + self._geometry_bytes)
                 incoming[self._bucket(slot.model.num_cells)].append(slot)
