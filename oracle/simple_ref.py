@@ -69,6 +69,28 @@ def geometry_from_mesh(mesh) -> dict:
     )
 
 
+def geometry_from_reference_arrays(d) -> dict:
+    """The same geometry dict from the arrays the reference's own mesh pass produced
+    (``Mesh.cell_properties`` / ``face_properties`` before ``finalize``, float32 as
+    preprocess/mesh.py computes them), as stored in tests/golden/ref_*.npz under
+    ``mesh_cell_*`` / ``mesh_face_*``."""
+    f64 = np.float64
+    i64 = np.int64
+    faces = d["mesh_cell_faces"].astype(i64)
+    return dict(
+        C=int(faces.shape[0]), K=int(d["mesh_face_unique_faces"].shape[0]), F=int(faces.shape[1]),
+        cell_faces=faces, normal=d["mesh_cell_normal"].astype(f64), cell_area=d["mesh_cell_area"].astype(f64),
+        neighbors=d["mesh_cell_neighbors"].astype(i64), face_side=d["mesh_cell_face_side"].astype(i64),
+        to_face=d["mesh_cell_cell_centroid_to_face_centroid"].astype(f64),
+        centroid=d["mesh_cell_centroids"].astype(f64), volume=d["mesh_cell_volumes"].astype(f64),
+        adjacent=d["mesh_face_adjacent_cells"].astype(i64), cell_face_index=d["mesh_face_cell_face_index"].astype(i64),
+        is_boundary=d["mesh_face_is_boundary"].astype(i64), face_centroid=d["mesh_face_centroid"].astype(f64),
+        distance=d["mesh_face_distance"].astype(f64), internal_ids=d["mesh_face_internal_face_ids"].astype(i64),
+        boundary_ids=d["mesh_face_boundary_face_ids"].astype(i64), nnz_per_cell=d["mesh_cell_nnz_per_cell"].astype(i64),
+        face_offset_index=d["mesh_cell_face_offset_index"].astype(i64), slot_valid=(faces >= 0),
+    )
+
+
 class Geometry:
     """Geometry cast to the working dtype, plus the per-face values init_structs derives.
 
@@ -103,8 +125,10 @@ def _dot(a, b, R):
     return float(np.dot(a.astype(R), b.astype(R)))
 
 
-def cg(A, b, x, invdiag, atol, maxiter, R=np.float64):
-    """Jacobi-preconditioned CG; stop when ||r||_2 <= atol (checked before each step)."""
+def cg(A, b, x, invdiag, atol, maxiter, R=np.float64, rtol=0.0):
+    """Jacobi-preconditioned CG; stop when ||r||_2 <= max(atol, rtol ||r_0||_2) (checked
+    before each step; the reference passes atol only, rtol is the relative stop of the
+    build's refinement sweeps, warpcfd_gb300/csrc/krylov.cu ``thr2``)."""
     T = x.dtype.type
     r = (b - A @ x).astype(T)
     rr = _dot(r, r, R)
@@ -112,7 +136,7 @@ def cg(A, b, x, invdiag, atol, maxiter, R=np.float64):
     rz = _dot(r, z, R)
     p = z.copy()
     k = 0
-    atol2 = atol * atol
+    atol2 = max(atol * atol, rtol * rtol * rr)
     while k < maxiter and rr > atol2:
         Ap = (A @ p).astype(T)
         pAp = _dot(p, Ap, R)
@@ -187,7 +211,8 @@ class OracleCase:
 
     def __init__(self, geo: dict, bc_type, bc_value, viscosity, density, *, T=np.float64, R=np.float64,
                  reference_cell=None, reference_value=0.0, correction=False, skew_correction=True,
-                 atol=None, maxiter=500, rhie_chow=False, explicit_internal=False, conv_scheme="upwind"):
+                 atol=None, maxiter=500, rhie_chow=False, explicit_internal=False, conv_scheme="upwind",
+                 p_refine=0, p_refine_rtol=1e-3):
         self.g = Geometry(geo, T)
         self.T, self.R = T, R
         g = self.g
@@ -203,6 +228,11 @@ class OracleCase:
         self.conv_scheme = conv_scheme
         self.atol = atol if atol is not None else (1e-5 if T == np.float32 else 1e-6)
         self.maxiter = maxiter
+        # precision form (not the reference's path): fp64 iterative refinement of the
+        # pressure solve, ``p_refine`` sweeps with a relative stop of ``p_refine_rtol`` each
+        self.p_refine = int(p_refine)
+        self.p_refine_rtol = float(p_refine_rtol)
+        self.p_x64 = None
         self.cell_values = np.zeros((C, 4), dtype=T)
         self.cell_gradients = np.zeros((C, 4, 3), dtype=T)
         self.face_values = np.zeros((K, 4), dtype=T)
@@ -494,6 +524,28 @@ class OracleCase:
         v = np.concatenate([vals[o] for o in range(3)])
         return sp.csr_matrix((v, (rows, cols)), shape=(3 * C, 3 * C))
 
+    def refined_pressure_solve(self, A, b, invdiag):
+        """The build's precision form of the pressure solve (warpcfd_gb300/csrc/capi.cu
+        ``wcfd_cg_refine``), not a reference step: ``p_refine`` sweeps of r = b - A x64 in
+        fp64 rounded once to the field type, a CG correction solve from zero to
+        ||r_k|| <= p_refine_rtol ||r||, x64 += d; the field solution is x64 rounded.  x64
+        persists across solves (started from the field solution on first use).  Returns
+        the total correction iterations and the fp64 residual norm of the result."""
+        T = self.T
+        if self.p_x64 is None:
+            self.p_x64 = self.p_x.astype(np.float64)
+        A64 = A.astype(np.float64)
+        b64 = b.astype(np.float64)
+        total = 0
+        for _ in range(self.p_refine):
+            r = (b64 - A64 @ self.p_x64).astype(T)
+            d = np.zeros_like(self.p_x)
+            k, _ = cg(A, r, d, invdiag, 0.0, self.maxiter, self.R, rtol=self.p_refine_rtol)
+            total += k
+            self.p_x64 += d.astype(np.float64)
+        self.p_x[:] = self.p_x64.astype(T)
+        return total, float(np.linalg.norm(b64 - A64 @ self.p_x64))
+
     # ---- one outer iteration / time step ----------------------------------------------
     def run(self, u_relax=0.7, p_relax=0.3, n_outer=1, n_inner=1, n_ortho=1, steady=True,
             n_time=1, dt=1.0, log=False):
@@ -548,7 +600,10 @@ class OracleCase:
                             prhs[rc, 0] = T(self.ref_value)
                         Apm = self.matrix(pv[0])
                         invp = jacobi_inverse(pv[0, self.diag_pos].copy())
-                        kp, rp = cg(Apm, prhs[:, 0].copy(), self.p_x, invp, self.atol, self.maxiter, self.R)
+                        if self.p_refine > 0:
+                            kp, rp = self.refined_pressure_solve(Apm, prhs[:, 0].copy(), invp)
+                        else:
+                            kp, rp = cg(Apm, prhs[:, 0].copy(), self.p_x, invp, self.atol, self.maxiter, self.R)
                         if steady and p_relax is not None:
                             a = T(p_relax)
                             self.cell_values[:, 3] = a * self.p_x + (T(1.0) - a) * self.cell_values[:, 3]

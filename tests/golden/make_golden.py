@@ -11,6 +11,20 @@ ldc64_fp32_500.npz       : the same case at the reference's own settings (fp32,
                            atol 1e-5, maxiter 500, 500 outer iterations) -- the numbers
                            the reference's configuration produces with this algorithm.
 ldc64_fp64_500.npz       : the same at fp64 with the reference's fp64 atol (1e-6).
+
+Fixed-iteration parity runs (the drop-in's parity bar: 500 iterations of the 64x64
+cavity, 100 of the 400x80 channel at Re 200 and 0.3 / 0.3, from zero fields), with the
+Krylov solves tightened so that the two sides compare the method, not where a loose
+stop happened to end a solve: momentum BiCGSTAB atol 1e-9 and the pressure solve by
+fp64 iterative refinement (4 sweeps, each a CG correction to a 1e-3 relative drop),
+maxiter 5000 (never reached):
+ldc64_fp32_500_refined.npz, channel400_fp32_100_refined.npz : fp32 fields (the method
+                           as the drop-in computes it);
+ldc64_fp64_500_refined.npz, channel400_fp64_100_refined.npz : fp64 fields, momentum atol
+                           1e-12, the same refinement in fp64 (the fp64 oracle of the
+                           same method).
+The channel fixtures store cell_values as float32 to keep the files small (the rounding,
+6e-8 relative, is far below the distances they are compared at).
 Each file stores cell_values (C,4) and the per-iteration Krylov counts.
 """
 import os
@@ -23,30 +37,53 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 from oracle.simple_ref import OracleCase, geometry_from_mesh  # noqa: E402
-from tests.cases import cavity_bc, cavity_mesh, host_boundary  # noqa: E402
+from tests.cases import cavity_bc, cavity_mesh, channel_bc, channel_mesh, host_boundary  # noqa: E402
 
+TIGHT = dict(maxiter=5000, p_refine=4, p_refine_rtol=1e-3)
 SPECS = {
     "ldc64_fp64_converged": dict(T=np.float64, atol=1e-10, iters=1500),
     "ldc64_fp32_converged": dict(T=np.float32, atol=1e-7, iters=1500),
     "ldc64_fp32_500": dict(T=np.float32, atol=1e-5, iters=500),
     "ldc64_fp64_500": dict(T=np.float64, atol=1e-6, iters=500),
+    "ldc64_fp32_500_refined": dict(T=np.float32, atol=1e-9, iters=500, **TIGHT),
+    "ldc64_fp64_500_refined": dict(T=np.float64, atol=1e-12, iters=500, **TIGHT),
+    "channel400_fp32_100_refined": dict(case="channel", T=np.float32, atol=1e-9, iters=100, store=np.float32,
+                                        **TIGHT),
+    "channel400_fp64_100_refined": dict(case="channel", T=np.float64, atol=1e-12, iters=100, store=np.float32,
+                                        **TIGHT),
 }
+
+
+def case_for(spec):
+    """(mesh, boundary, nu, reference cell, (u_relax, p_relax)) of a fixture's case."""
+    if spec.get("case", "cavity") == "cavity":
+        m = cavity_mesh(64)
+        return m, host_boundary(m, cavity_bc), 0.01, 0, (0.7, 0.3)
+    m = channel_mesh(400, 80)
+    return m, host_boundary(m, channel_bc), 1.0 / 200.0, None, (0.3, 0.3)
 
 
 def make(name):
     spec = SPECS[name]
-    m = cavity_mesh(64)
-    b = host_boundary(m, cavity_bc)
-    oc = OracleCase(geometry_from_mesh(m), b.boundary_type, b.boundary_values, 0.01, 1.0, T=spec["T"],
-                    reference_cell=0, atol=spec["atol"])
+    m, b, nu, ref, relax = case_for(spec)
+    oc = OracleCase(geometry_from_mesh(m), b.boundary_type, b.boundary_values, nu, 1.0, T=spec["T"],
+                    reference_cell=ref, atol=spec["atol"], maxiter=spec.get("maxiter", 500),
+                    p_refine=spec.get("p_refine", 0), p_refine_rtol=spec.get("p_refine_rtol", 1e-3))
     t = time.time()
-    oc.run(0.7, 0.3, n_outer=spec["iters"], log=True)
+    oc.run(*relax, n_outer=spec["iters"], log=True)
     krylov = np.array([(a, c) for a, _, c in oc.log], dtype=np.int32)
-    np.savez_compressed(os.path.join(HERE, name + ".npz"), cell_values=oc.cell_values.astype(np.float64),
+    np.savez_compressed(os.path.join(HERE, name + ".npz"),
+                        cell_values=oc.cell_values.astype(spec.get("store", np.float64)),
                         krylov=krylov, atol=spec["atol"], iters=spec["iters"])
-    print(name, f"{time.time() - t:.1f}s")
+    print(name, f"{time.time() - t:.1f}s", "krylov max", krylov.max(0))
 
 
 if __name__ == "__main__":
-    for n in (sys.argv[1:] or list(SPECS)):
-        make(n)
+    names = sys.argv[1:] or list(SPECS)
+    if len(names) > 1:
+        import multiprocessing as mp
+
+        with mp.get_context("spawn").Pool(min(len(names), os.cpu_count() or 1)) as pool:
+            pool.map(make, names)
+    else:
+        make(names[0])
