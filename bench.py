@@ -1,12 +1,16 @@
 """Benchmark of the SIMPLE outer iteration (cell-iterations/s) on GB300.
 
-Default workload: steady channel flow, 400 x 80 x 1 hexes on a 10 x 1 domain, uniform
-inlet u = 1, outlet p = 0, no-slip walls, Re = 200, relaxation 0.3 / 0.3, fp32 fields
-with fp64 Krylov reductions.  One step = one SIMPLE outer iteration (momentum BiCGSTAB +
-pressure CG, up to 500 iterations each, atol 1e-5).  Synthetic seeded mesh, zero
-initial fields.
+Default workload: the 3D lid-driven cavity, 128^3 hexes (2,097,152 cells) in a unit box,
+lid u = 1, Re = 400, relaxation 0.7 / 0.3, fp32 fields and matrices with float-float
+(fp64-class) Krylov reductions -- the single large case the roofline is measured on.
+One step = one SIMPLE outer iteration (momentum BiCGSTAB + pressure CG, up to 500
+iterations each, atol 1e-5).  Synthetic seeded mesh (built by the GPU mesh pass), zero
+initial fields.  The same JSON line carries a ``serving`` block: the serving mix (1,024
+steady cavity/channel requests, seeded Poisson arrivals) through the continuous-batching
+server, with the drop-in path run one case at a time on a stratified sample of the same
+mix for ``batched_over_drop_in`` (``--no-serving`` leaves it out).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload channel|cavity|cavity3d]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload cavity3d|channel|cavity|cylinder|serve]
   python bench.py --impl reference ...   # the CPU restatement of the reference algorithm
 
 Timing: W untimed steps, then K steps, each bracketed by CUDA events on the solver
@@ -243,9 +247,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(rows)}
 
 
+def cpu_warmup_steps(mesh, requested=3):
+    """Untimed oracle steps before a CPU timing: none on meshes of a million cells or more
+    (one outer iteration of the 128^3 cavity is ~30 s of numpy; a CPU has no warm-up
+    beyond the first step's allocations, which the timed sample then includes)."""
+    return 0 if mesh.num_cells >= 1_000_000 else requested
+
+
 def cpu_baseline(workload, mesh, seconds=15.0, warm=3):
     """The oracle (fp32, the same algorithm) on this host: ``warm`` untimed outer
-    iterations from zero fields, then as many timed ones as fit in ~``seconds``."""
+    iterations from zero fields, then as many timed ones as fit in ~``seconds`` (at least
+    one)."""
+    warm = cpu_warmup_steps(mesh, warm)
     oc = build_oracle_case(workload, mesh)
     oracle_step(oc, workload, warm)
     t0 = time.perf_counter()
@@ -256,9 +269,9 @@ def cpu_baseline(workload, mesh, seconds=15.0, warm=3):
         if time.perf_counter() - t0 > seconds:
             break
     dt = time.perf_counter() - t0
-    return {"value": mesh.num_cells * n / dt, "unit": METRIC, "cores": 1, "kind": "port",
+    return {"value": mesh.num_cells * n / dt, "unit": METRIC, "cores": 1, "nproc": os.cpu_count(), "kind": "port",
             "sample": f"{n} SIMPLE outer iterations (after {warm} untimed) of the same {workload} case, numpy/scipy "
-                      f"fp32 restatement (oracle/simple_ref.py), single thread"}
+                      f"fp32 restatement (oracle/simple_ref.py), single thread ({os.cpu_count()} host cores)"}
 
 
 def fp64_field_error(workload, mesh, steps=20):
@@ -298,13 +311,27 @@ def fp64_field_error(workload, mesh, steps=20):
             "oracle_seconds": round(time.perf_counter() - t0, 2)}
 
 
+def warp_probe():
+    """Whether warp-lang (the reference's runtime, not vendored) can be imported here."""
+    import importlib.util
+
+    if importlib.util.find_spec("warp") is None:
+        return {"warp_available": False, "why": "importlib.util.find_spec('warp') is None"}
+    try:
+        import warp
+        return {"warp_available": True, "version": getattr(warp, "__version__", "?")}
+    except Exception as e:  # noqa: BLE001 - any import failure is the answer
+        return {"warp_available": False, "why": f"import warp failed: {e!r}"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
     mesh = build_mesh(args.workload)
     oc = build_oracle_case(args.workload, mesh)
-    oracle_step(oc, args.workload, args.warmup)
+    warm = cpu_warmup_steps(mesh, args.warmup)
+    oracle_step(oc, args.workload, warm)
     # each step is one full outer iteration of the workload; stop early (and say so) if
     # the K steps would not end within --ref-seconds
     t0 = time.perf_counter()
@@ -316,39 +343,42 @@ def run_reference(args):
             break
     dt = time.perf_counter() - t0
     v = mesh.num_cells * done / dt
+    probe = warp_probe()
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus,
-            "steps": done, "steps_requested": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / done,
+            "steps": done, "steps_requested": args.steps, "warmup": args.warmup, "warmup_run": warm,
+            "ms_per_step": 1e3 * dt / done,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": WORKLOADS[args.workload], "cells": mesh.num_cells},
-            "cpu_baseline": {"value": v, "unit": METRIC, "cores": 1, "kind": "port",
-                             "sample": f"{done} SIMPLE outer iterations after {args.warmup} untimed, numpy/"
-                                       "scipy fp32 restatement of the reference algorithm (warp-lang is not "
-                                       "installable here), single thread"},
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": 1, "nproc": os.cpu_count(), "kind": "port",
+                             "sample": f"{done} SIMPLE outer iterations after {warm} untimed, numpy/"
+                                       "scipy fp32 restatement of the reference algorithm, single thread "
+                                       f"({os.cpu_count()} host cores); the reference itself needs warp-lang: "
+                                       f"{probe}"},
+            "reference_runtime": probe,
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
 
 
-def run_serve(args):
-    """Serving mix through the continuous-batching server; the drop-in path (one case at a
-    time, same settings) runs a bounded sample of the same mix for the comparison.  Under
-    torchrun each rank serves its round-robin share of the mix on its own GPU (replicas, no
-    collective on the data path); rank 0 prints the whole-job figures."""
+def stratified_sample(reqs, n):
+    """``n`` requests spread evenly over the mix sorted by (kind, cells): each kind keeps
+    its share and each kind's sizes their spread (evenly spaced quantiles)."""
+    order = sorted(reqs, key=lambda r: (r.kind, r.cells, r.rid))
+    if n >= len(order):
+        return order
+    idx = np.unique(np.linspace(0, len(order) - 1, n).round().astype(np.int64))
+    return [order[i] for i in idx]
+
+
+def serve_mix(args, local, rank=0, world=1, dist=None):
+    """The serving mix through the continuous-batching server (this rank's round-robin
+    share), then the drop-in path one case at a time on a stratified sample of the same
+    share with the same stop settings.  Returns the whole-job figures."""
     import torch
 
-    from warpcfd_gb300.build import build_library
     from warpcfd_gb300.replicas import max_over_ranks, shard, sum_over_ranks
     from warpcfd_gb300.serve import Server, make_request_mix, run_drop_in
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    build_library()
     reqs_all = make_request_mix(args.requests, seed=0, rate=args.rate)
     reqs = shard(reqs_all, rank, world)
     # warm-up: a few small requests touch every kernel and the caches
@@ -362,25 +392,58 @@ def run_serve(args):
     wall = max_over_ranks(summ["wall_s"])
     cell_its = sum_over_ranks(rep.cell_iterations)
     value = cell_its / wall
-    # drop-in on a sample: the first requests of this rank's share, same stop settings
-    n_drop = min(args.drop_in_sample, len(reqs))
-    drop = run_drop_in(reqs[:n_drop], max_outer=args.max_outer)
+    sample = stratified_sample(reqs, min(args.drop_in_sample, len(reqs)))
+    drop = run_drop_in(sample, max_outer=args.max_outer)
     drop_rate = sum_over_ranks(drop["cell_iterations_per_s"]) / world
+    by_kind = {k: sum(r.kind == k for r in sample) for k in ("cavity", "channel")}
+    mix_kind = {k: sum(r.kind == k for r in reqs) for k in ("cavity", "channel")}
+    drop_status = {}
+    for _, _, r in drop["results"]:
+        st = "converged" if r < 1e-6 else ("diverged" if not np.isfinite(r) else "exhausted")
+        drop_status[st] = drop_status.get(st, 0) + 1
+    return {
+        "value": value, "wall": wall, "requests": len(reqs_all), "serving": summ, "clocks": clocks.summary(),
+        "drop_in": {"requests_per_rank": len(sample), "sample": "stratified: evenly spaced over the mix sorted by "
+                    "(kind, cells)", "sample_kinds": by_kind, "mix_kinds": mix_kind,
+                    "sample_cells_median": float(np.median([r.cells for r in sample])),
+                    "mix_cells_median": float(np.median([r.cells for r in reqs])),
+                    "cell_iterations_per_s": drop_rate, "wall_s": drop["wall_s"], "status": drop_status},
+        "batched_over_drop_in": value / world / max(drop_rate, 1e-9),
+    }
+
+
+def run_serve(args):
+    """Serving mix through the continuous-batching server; the drop-in path (one case at a
+    time, same settings) runs a stratified sample of the same mix for the comparison.
+    Under torchrun each rank serves its round-robin share of the mix on its own GPU
+    (replicas, no collective on the data path); rank 0 prints the whole-job figures."""
+    import torch
+
+    from warpcfd_gb300.build import build_library
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    build_library()
+    out = serve_mix(args, local, rank, world, dist)
     if dist is not None:
         dist.destroy_process_group()
     if rank != 0:
         return 0
     line = {
-        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": len(reqs_all),
-        "warmup": 4, "ms_per_step": 1e3 * wall / max(len(reqs_all), 1), "higher_is_better": True,
+        "metric": METRIC, "value": out["value"], "unit": METRIC, "n_gpus": world, "steps": out["requests"],
+        "warmup": 4, "ms_per_step": 1e3 * out["wall"] / max(out["requests"], 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOADS["serve"], "requests": len(reqs_all), "arrival_rate_per_s": args.rate,
+        "config": {"workload": WORKLOADS["serve"], "requests": out["requests"], "arrival_rate_per_s": args.rate,
                    "max_outer": args.max_outer, "step": "one request served to completion",
                    "parallelism": f"request shards x{world}"},
-        "serving": summ,
-        "drop_in": {"requests_per_rank": n_drop, "cell_iterations_per_s": drop_rate, "wall_s": drop["wall_s"]},
-        "batched_over_drop_in": value / world / max(drop_rate, 1e-9),
-        "clocks": clocks.summary(),
+        "serving": out["serving"], "drop_in": out["drop_in"], "batched_over_drop_in": out["batched_over_drop_in"],
+        "clocks": out["clocks"],
     }
     print(json.dumps(line))
     return 0
@@ -518,11 +581,23 @@ def run_ours(args):
                      "step_bytes_per_s_GBs": float(np.sum(step_bytes) / (total_ms * 1e-3) / 1e9)},
         "kernel_ms": {"bicgstab": float(bicg_ms.mean()), "cg": float(cg_ms.mean()), "step": float(step_ms.mean())},
     }
+    if traffic is not None:
+        # the same launch judged by the DRAM bytes ncu measured for it instead of the
+        # algorithmic bytes (below 1 x algorithmic: the vectors hit L2)
+        line["roofline"]["achieved_dram"] = traffic / (kms / nl * 1e-3) / 1e9
+        line["roofline"]["frac_dram"] = line["roofline"]["achieved_dram"] / peak
     if rank == 0:
         line["clocks"] = clocks.summary()
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(args.workload, mesh, seconds=args.cpu_seconds)
             line["fp64_oracle"] = fp64_field_error(args.workload, mesh)
+    if world == 1 and args.workload == "cavity3d" and not args.no_serving:
+        # the serving half of the metric (p50/p99 time to a converged solution, batched
+        # over drop-in), on the same GPU after the 128^3 case is released
+        del model, solver, snap, flush
+        torch.cuda.empty_cache()
+        line["serving"] = serve_mix(args, local)
+    if rank == 0:
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
@@ -535,12 +610,13 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="channel", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="cavity3d", choices=sorted(WORKLOADS))
     ap.add_argument("--p-refine", type=int, default=None,
                     help="fp64 refinement sweeps of the pressure solve (default: 3 for cylinder, else 0)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ref-seconds", type=float, default=150.0)
+    ap.add_argument("--ref-seconds", type=float, default=90.0)
+    ap.add_argument("--no-serving", action="store_true", help="leave the serving block out of the default line")
     ap.add_argument("--no-clocks", action="store_true", help="do not sample nvidia-smi during the timed region")
     ap.add_argument("--requests", type=int, default=1024, help="serve workload: requests in the mix")
     ap.add_argument("--max-active", type=int, default=256, help="serve workload: cases in flight at most")
