@@ -22,6 +22,18 @@ __device__ __forceinline__ unsigned cluster_nranks() {
 __device__ __forceinline__ void cluster_sync_all() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
+// The cluster barrier of a reduction: warp 0 (which made the remote slot stores) arrives
+// with release semantics, the other warps arrive relaxed, every thread waits with acquire.
+// Everything the other warps wrote before the CTA's last __syncthreads happens before
+// warp 0's release (the CTA barrier orders it, and the release is cumulative), so the
+// other CTAs see it after their wait; a release by 32 instead of 1,024 threads.
+__device__ __forceinline__ void cluster_sync_warp0_release() {
+    if (threadIdx.x < 32)
+        asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    else
+        asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
 // shared::cluster address of `p` (a pointer into this CTA's shared memory) in CTA `rank`
 __device__ __forceinline__ uint32_t map_rank(const void* p, unsigned rank) {
     const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
@@ -51,9 +63,9 @@ __device__ __forceinline__ void st_cluster_v2f32(uint32_t addr, float a, float b
 // stores its values into sbuf [NV][CBS]; threads 0..255 merge four each ((t + t+256) +
 // (t+512 + t+768), a pairwise tree so the merges overlap); warp 0 merges eight each
 // (l, l+32, ..., l+224, again pairwise), then by butterfly, and stores the CTA total into
-// slot `me` of every CTA (DSMEM); after the cluster barrier warp 0 merges the cs <= 16
-// slots in rank order (four butterfly levels).  One cluster barrier and two
-// __syncthreads; slots [2][NV][16] are double-buffered by `parity`.
+// slot `me` of every CTA (DSMEM); after the cluster barrier (release by warp 0 only)
+// warp 0 merges the cs <= 16 slots in rank order (four butterfly levels).  One cluster
+// barrier and two __syncthreads; slots [2][NV][16] are double-buffered by `parity`.
 template <int NV>
 __device__ __forceinline__ void cluster_reduce_tree(const ff (&acc)[NV], ff (&out)[NV], ff* sbuf, ff* slots,
                                                     unsigned parity, unsigned me, unsigned cs) {
@@ -92,7 +104,7 @@ __device__ __forceinline__ void cluster_reduce_tree(const ff (&acc)[NV], ff (&ou
             if ((unsigned)t < cs) st_cluster_v2f32(map_rank(slots + (parity * NV + i) * 16 + me, t), x.hi, x.lo);
         }
     }
-    cluster_sync_all();
+    cluster_sync_warp0_release();
     if (t < 32) {
 #pragma unroll
         for (int i = 0; i < NV; ++i) {
