@@ -305,6 +305,52 @@ int wcfd_krylov_solve(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_w
 int wcfd_cg_noalloc(const wcfd_mesh* m, wcfd_system A, float* x, double atol, int32_t maxiter,
                     wcfd_solve_stats* stats, void* stream);
 
+/* ------------------------------------------------------------------ Term / Equation API
+ * The reference's terms form weight arrays on the device and Equation adds them into its
+ * matrix (warp_cfd/FV/terms/*.py, FV/kernels/equation_kernels.py:52-122).  Layouts as the
+ * reference's: face-based weights [C][F][n][3] (owner coefficient, neighbour coefficient,
+ * explicit part of cell c's side of the face in slot f), cell-based [C][n][2] (diagonal,
+ * explicit part), explicit grad weights [C*3].  Every entry is written by one thread
+ * (the cell's side of the face), so no atomics; all pointers are DEVICE pointers. */
+typedef struct wcfd_term_fields {
+    int32_t n;          /* fields of the term, 1..3 */
+    int32_t index[3];   /* their columns of cell_values (u v w p = 0 1 2 3) */
+} wcfd_term_fields;
+
+/* ConvectionTerm.calculate_weights (terms/convection.py:43-91): scheme 0 upwind, 1 central
+ * difference, 2 upwindLinear (Implicit_Schemes/convectionScheme.py:3-88), skew correction
+ * in the explicit part as the reference's term always applies it. */
+int wcfd_convection_weights(const wcfd_mesh* m, wcfd_state s, wcfd_term_fields f, int32_t scheme, float* weights,
+                            void* stream);
+/* DiffusionTerm.calculate_weights (terms/diffusion.py:113-198): viscosity nu, or one value
+ * per face in nu_faces (device, K) when not NULL; corrected = the non-orthogonal scheme
+ * (laplacianScheme.py:39-67); bc_mode 0 = the boundary table, 1 = every boundary face a
+ * fixed normal gradient bc_value (the term's von_neumann / dirchlet options). */
+int wcfd_diffusion_weights(const wcfd_mesh* m, wcfd_bc bc, wcfd_state s, wcfd_term_fields f, float nu,
+                           const float* nu_faces, int32_t corrected, int32_t bc_mode, float bc_value, float* weights,
+                           void* stream);
+/* DdtTerm.calculate_weights, backward Euler (terms/ddt.py:24-32) */
+int wcfd_ddt_weights(const wcfd_mesh* m, wcfd_state s, wcfd_term_fields f, float dt, float* weights, void* stream);
+/* GradTerm.calculate_weights (terms/grad.py:20-29): grad(field) V, rows 3c + d */
+int wcfd_grad_weights(const wcfd_mesh* m, wcfd_state s, int32_t field, float* weights, void* stream);
+
+/* one implicit term of an assembly: its device weights and its (assigned) scale */
+typedef struct wcfd_term {
+    const float* weights;
+    float        scale;
+    int32_t      cell_based;   /* 1: [C][n][2] weights, 0: [C][F][n][3] */
+} wcfd_term;
+#define WCFD_MAX_TERMS 8
+/* Equation.form_system (terms/equation.py:99-125) over any list of implicit terms (host
+ * array of n_terms <= WCFD_MAX_TERMS): the system (ncomp = the terms' field count) is
+ * overwritten with the sum of the terms, cell-parallel and atomic-free; explicit weights
+ * of internal faces do not reach the RHS, as in the reference (Q1).  The off-diagonals are
+ * stored once for all components: they are taken from component 0 (every scheme's
+ * neighbour coefficient is the same for all fields). */
+int wcfd_assemble_terms(const wcfd_mesh* m, wcfd_system A, const wcfd_term* terms, int32_t n_terms, void* stream);
+/* Equation.add_RHS (terms/equation.py:167-168): rhs[i] += scale arr[i], i < n (device) */
+int wcfd_add_rhs(float* rhs, const float* arr, float scale, int64_t n, void* stream);
+
 /* ------------------------------------------------------------------ fused steps */
 /* One steady SIMPLE outer iteration (incompressible.py:95-156 with steady_state=True),
  * or one PISO time step (NUM_OUTER_LOOPS = 1, steady_state=False), as a fixed sequence of
@@ -344,7 +390,10 @@ typedef struct wcfd_batch_dims {
                                 on it: those kernels compute each face or cell alone)  */
     int32_t explicit_terms;  /* OR of the cases' wcfd_params.explicit_terms: non-zero
                                 selects the assembly kernels with those terms compiled in */
-    int32_t pad_;
+    int32_t p_refine;        /* fp64 iterative-refinement sweeps of every case's pressure
+                                solve (each: residual in fp64 from p_x64, a correction CG to
+                                the case's p_refine_rtol, p_x64 += correction); 0 = the
+                                plain solve.  Every case then needs p_x64 and p_work. */
 } wcfd_batch_dims;
 
 /* Cluster size wcfd_batch_simple_iteration would pick for these dims (0 = no cluster

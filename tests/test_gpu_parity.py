@@ -478,8 +478,9 @@ def test_cluster_cg_at_its_size_limit():
 
 @pytest.mark.parametrize("steady", [True, False])
 def test_term_equation_api_matches_fused_assembly(steady):
-    """The reference's Term/Equation API (form_system, relax, add_RHS, replace_row) builds the
-    same momentum and pressure systems, bit for bit, as the fused solver assembly."""
+    """The reference's Term/Equation API (terms forming their weights, form_system, relax,
+    add_RHS, replace_row) builds the same momentum and pressure systems as the fused solver
+    assembly, to rounding (the generic assembly adds the terms' weights in another order)."""
     m = cavity_mesh(12, jitter=0.1, seed=6)
     model, solver, oc = make_pair(m, cavity_bc, steady=steady, dt=0.01)
     _seed_state(model, oc, 7)
@@ -505,7 +506,7 @@ def test_term_equation_api_matches_fused_assembly(steady):
                        explicit_terms=-inv_density * solver.grad_P, fvm=model)
     torch.cuda.synchronize()
     for a, b in zip(fused, (ve.diag, ve.off, ve.rhs)):
-        assert torch.equal(a, b)
+        assert rel_l2(b.cpu().numpy(), a.cpu().numpy()) < 1e-6
     # pressure: form_system + add_RHS(div) + replace_row, against the fused pressure assembly
     rua_f = torch.rand(m.num_faces, device="cuda") + 0.1
     solver.rUA_faces.copy_(rua_f)
@@ -521,7 +522,7 @@ def test_term_equation_api_matches_fused_assembly(steady):
     pe.replace_row(model.reference_pressure_cell_id, float(model.reference_pressure))
     torch.cuda.synchronize()
     for a, b in zip(fused, (pe.diag, pe.off, pe.rhs)):
-        assert torch.allclose(a, b, rtol=0, atol=0) or torch.equal(a, b)
+        assert rel_l2(b.cpu().numpy(), a.cpu().numpy()) < 1e-6
 
 
 def _reference_style_iteration(model, solver):

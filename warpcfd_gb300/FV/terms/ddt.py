@@ -1,5 +1,10 @@
-"""DdtTerm (warp_cfd/FV/terms/ddt.py:7-32): backward Euler V/dt on the diagonal and
-phi_old V/dt on the RHS, formed in the momentum assembly kernel when steady_state=False."""
+"""DdtTerm (warp_cfd/FV/terms/ddt.py:7-32): backward Euler.  Calling the term with the time
+step forms its (C, n, 2) weights (V/dt, -phi V/dt) on the device (wcfd_ddt_weights)."""
+import ctypes as ct
+
+import torch
+
+from ... import _lib
 from .terms import Term
 
 
@@ -12,7 +17,11 @@ class DdtTerm(Term):
         self.dt = None
 
     def calculate_weights(self, fv, dt=None, **kwargs):
-        """Records the time step of the next form_system (ddt.py:24-32)."""
         if dt is not None:
             self.dt = float(dt)
+        if self.dt is None:
+            raise ValueError("call the ddt term with its time step: ddt(model, dt=dt)")
+        w = self._weights_for(fv)
+        _lib.call("wcfd_ddt_weights", ct.byref(fv.mesh_struct()), fv.state_struct(), self.field_struct(),
+                  float(self.dt), ct.c_void_p(w.data_ptr()), ct.c_void_p(torch.cuda.current_stream().cuda_stream))
         return self

@@ -118,79 +118,37 @@ class Equation:
         return self.matrix.to_dense()
 
     # ------------------------------------------------------------------ assembly (equation.py:99-194)
-    def form_system(self, implicit_terms, explicit_terms=None, fvm=None):
-        """Assemble the system from terms (equation.py:99-165), on the fused kernels:
-
-        * three velocity fields: ``[convection, -diffusion]`` (steady) or
-          ``[ddt, convection, -diffusion]`` (transient) with ``explicit_terms =
-          -inv_density * grad_P``, upwind (or upwindLinear, whose internal explicit part the
-          reference drops) or central-difference convection and a scalar viscosity set by calling
-          the diffusion term (``diffusion(model, viscosity=nu)``) -> wcfd_assemble_momentum
-          without relaxation (call ``relax`` next, as the reference does);
-        * one field: a diffusion term of scale +1 with a scalar or per-face viscosity ->
-          wcfd_assemble_pressure with a zero right-hand side source (``add_RHS`` and
-          ``replace_row`` then act as in the reference).
-
-        Other term combinations raise NotImplementedError."""
-        from .convection import ConvectionTerm
-        from .ddt import DdtTerm
-        from .diffusion import DiffusionTerm
-        from .grad import GradTerm
-
+    def form_system(self, implicit_terms=None, explicit_terms=None, *, fvm=None):
+        """Assemble the system from terms (equation.py:99-125): any list of implicit terms,
+        face-based (convection, diffusion) or cell-based (ddt), each with its assigned scale,
+        added by one cell-parallel, atomic-free kernel (wcfd_assemble_terms), then every
+        explicit term's weights times its scale added to the right-hand side.  Each term must
+        have been called (``term(model, ...)``) so that its weights are current.  The
+        system is overwritten (the reference resets it first, equation.py:202-204)."""
         fvm = self.fvm if fvm is None else fvm
-        terms = list(implicit_terms) if isinstance(implicit_terms, (list, tuple)) else [implicit_terms]
-        conv = [t for t in terms if isinstance(t, ConvectionTerm)]
-        diff = [t for t in terms if isinstance(t, DiffusionTerm)]
-        ddt = [t for t in terms if isinstance(t, DdtTerm)]
-        if len(diff) != 1 or len(conv) > 1 or len(ddt) > 1 or len(conv) + len(diff) + len(ddt) != len(terms):
-            raise NotImplementedError("form_system takes one diffusion term, with at most one convection and "
-                                      "one ddt term")
-        d = diff[0]
-        if d.viscosity is None:
-            raise ValueError("call the diffusion term with its viscosity first: diffusion(model, viscosity=nu)")
-        C, K = fvm.num_cells, fvm.num_faces
-        dev = fvm.device
-        if getattr(self, "_rua_scratch", None) is None:
-            self._rua_scratch = torch.zeros(C, dtype=torch.float32, device=dev)
-            self._div_zero = torch.zeros(C, dtype=torch.float32, device=dev)
-        null = _lib.System_t(None, None, None, 1, 0)
+        terms = [] if implicit_terms is None else (list(implicit_terms) if isinstance(implicit_terms, (list, tuple))
+                                                   else [implicit_terms])
+        if len(terms) > _lib.MAX_TERMS:
+            raise ValueError(f"at most {_lib.MAX_TERMS} implicit terms")
+        arr = (_lib.Term_t * max(len(terms), 1))()
+        for i, t in enumerate(terms):
+            if not t.implicit:
+                raise AssertionError("form_system's implicit_terms must be implicit terms")
+            if t.num_outputs != self.num_outputs:
+                raise ValueError(f"a term of {t.num_outputs} fields in a system of {self.num_outputs}")
+            if t.weights is None:
+                raise ValueError("call the term first (term(model, ...)) so that its weights exist")
+            arr[i] = _lib.Term_t(t.weights.data_ptr(), float(t.scale), int(bool(t.cell_based)))
         stream = ct.c_void_p(torch.cuda.current_stream().cuda_stream)
-        if self.num_outputs == 3:
-            ex = [] if explicit_terms is None else (list(explicit_terms) if isinstance(explicit_terms, (list, tuple))
-                                                    else [explicit_terms])
-            grads = [t for t in ex if isinstance(t, GradTerm)]
-            if len(conv) != 1 or conv[0].interpolation not in _lib.CONVECTION or conv[0].scale != 1.0 \
-                    or d.scale != -1.0 or len(grads) != 1 or len(ex) != 1 or grads[0].scale >= 0.0 \
-                    or (ddt and ddt[0].scale != 1.0):
-                raise NotImplementedError("the momentum system is [ddt,] convection (upwind, upwindLinear or "
-                                          "central difference) - diffusion with the explicit source -(1/rho) grad p")
-            if torch.is_tensor(d.viscosity):
-                raise NotImplementedError("the momentum viscosity is a scalar")
-            steady = not ddt
-            if not steady and ddt[0].dt is None:
-                raise ValueError("call the ddt term with its time step first: ddt(model, dt=dt)")
-            rho = -1.0 / grads[0].scale
-            prm = _lib.Params_t(float(d.viscosity), float(rho), 0.0, 0.0, float(ddt[0].dt) if ddt else 1.0, 0.0, -1,
-                                int(steady), 1, 1, self.max_iter, int(bool(fvm.skew_correction)), float(self.tol),
-                                float(self.tol), 0, 0, 1e-3, 0.0, 0.0, 0, _lib.CONVECTION[conv[0].interpolation])
-            case = _lib.Case_t(fvm.mesh_struct(d.correction), fvm.bc_struct(), fvm.state_struct(),
-                               self.system_struct(), null, None, None, self._rua_scratch.data_ptr(), None, None,
-                               None, None, _lib.KrylovWS_t(), _lib.KrylovWS_t(), None, prm, None)
-            _lib.call("wcfd_assemble_momentum", ct.byref(case), stream)
-            return
-        if conv or ddt or d.scale != 1.0:
-            raise NotImplementedError("a scalar system is a diffusion term of scale +1")
-        nu = d.viscosity
-        nu_f = nu if torch.is_tensor(nu) else torch.full((K,), float(nu), dtype=torch.float32, device=dev)
-        if nu_f.numel() != K:
-            raise ValueError("a per-face viscosity has one value per face")
-        nu_f = nu_f.to(torch.float32).contiguous()
-        prm = _lib.Params_t(1.0, 1.0, 0.0, 0.0, 1.0, 0.0, -1, 1, 1, 1, self.max_iter,
-                            int(bool(fvm.skew_correction)), float(self.tol), float(self.tol), 0, 0, 1e-3, 0.0, 0.0)
-        case = _lib.Case_t(fvm.mesh_struct(d.correction), fvm.bc_struct(), fvm.state_struct(), null,
-                           self.system_struct(), None, None, None, nu_f.data_ptr(), self._div_zero.data_ptr(), None,
-                           None, _lib.KrylovWS_t(), _lib.KrylovWS_t(), None, prm, None)
-        _lib.call("wcfd_assemble_pressure", ct.byref(case), stream)
+        _lib.call("wcfd_assemble_terms", ct.byref(fvm.mesh_struct()), self.system_struct(), arr, len(terms), stream)
+        ex = [] if explicit_terms is None else (list(explicit_terms) if isinstance(explicit_terms, (list, tuple))
+                                                else [explicit_terms])
+        for t in ex:
+            if t.implicit:
+                raise AssertionError("explicit_terms must be explicit terms")
+            if t.weights is None:
+                raise ValueError("call the term first (term(model, ...)) so that its weights exist")
+            self.add_RHS(t.weights, t.scale)
 
     def relax(self, relaxation_factor, fvm=None):
         """Implicit relaxation on the diagonal (equation.py:173-182)."""
@@ -214,7 +172,14 @@ class Equation:
             _lib.call("wcfd_replace_row", ct.byref(m), self.system_struct(), int(r), float(v), stream)
 
     def add_RHS(self, arr, scale=1.0):
-        self.rhs += arr.reshape(-1) * float(scale)
+        """rhs += scale arr (equation.py:167-168), on the device (wcfd_add_rhs)."""
+        a = arr.reshape(-1)
+        if a.numel() != self.rhs.numel():
+            raise ValueError(f"add_RHS: {a.numel()} values for a right-hand side of {self.rhs.numel()}")
+        if a.dtype != torch.float32 or not a.is_contiguous() or a.device != self.rhs.device:
+            a = a.to(device=self.rhs.device, dtype=torch.float32).contiguous()
+        _lib.call("wcfd_add_rhs", ct.c_void_p(self.rhs.data_ptr()), ct.c_void_p(a.data_ptr()), float(scale),
+                  int(a.numel()), ct.c_void_p(torch.cuda.current_stream().cuda_stream))
 
     def reset(self):
         self.rhs.zero_()

@@ -89,7 +89,18 @@ class BatchDims_t(ct.Structure):
     _fields_ = [("max_cells", ct.c_int32), ("max_faces", ct.c_int32), ("faces_per_cell", ct.c_int32),
                 ("ell_width", ct.c_int32), ("n_inner", ct.c_int32), ("n_ortho", ct.c_int32),
                 ("cluster_size", ct.c_int32), ("field_block", ct.c_int32), ("explicit_terms", ct.c_int32),
-                ("pad_", ct.c_int32)]
+                ("p_refine", ct.c_int32)]
+
+
+class TermFields_t(ct.Structure):
+    _fields_ = [("n", ct.c_int32), ("index", ct.c_int32 * 3)]
+
+
+class Term_t(ct.Structure):
+    _fields_ = [("weights", vp), ("scale", ct.c_float), ("cell_based", ct.c_int32)]
+
+
+MAX_TERMS = 8
 
 
 class MeshCells_t(ct.Structure):
@@ -125,6 +136,13 @@ _SIGS = {
     "wcfd_rua": (ct.c_int, [ct.POINTER(Mesh_t), vp, ct.c_float, vp, vp]),
     "wcfd_hbya_add": (ct.c_int, [ct.c_int32, vp, vp, vp, vp]),
     "wcfd_relax": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, ct.c_int32, ct.c_float, vp]),
+    "wcfd_convection_weights": (ct.c_int, [ct.POINTER(Mesh_t), State_t, TermFields_t, ct.c_int32, vp, vp]),
+    "wcfd_diffusion_weights": (ct.c_int, [ct.POINTER(Mesh_t), BC_t, State_t, TermFields_t, ct.c_float, vp, ct.c_int32,
+                                          ct.c_int32, ct.c_float, vp, vp]),
+    "wcfd_ddt_weights": (ct.c_int, [ct.POINTER(Mesh_t), State_t, TermFields_t, ct.c_float, vp, vp]),
+    "wcfd_grad_weights": (ct.c_int, [ct.POINTER(Mesh_t), State_t, ct.c_int32, vp, vp]),
+    "wcfd_assemble_terms": (ct.c_int, [ct.POINTER(Mesh_t), System_t, ct.POINTER(Term_t), ct.c_int32, vp]),
+    "wcfd_add_rhs": (ct.c_int, [vp, vp, ct.c_float, ct.c_int64, vp]),
     "wcfd_replace_row": (ct.c_int, [ct.POINTER(Mesh_t), System_t, ct.c_int32, ct.c_float, vp]),
     "wcfd_krylov_solve": (ct.c_int, [ct.POINTER(Mesh_t), System_t, vp, KrylovWS_t, ct.c_int32, ct.c_double,
                                      ct.c_double, ct.c_int32, vp, vp]),

@@ -19,7 +19,8 @@ CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
 LIB = PKG / "libwcfd.so"
 BUILD_DIR = PKG / "_build"
-SOURCES = ["fields.cu", "assemble.cu", "krylov.cu", "krylov_cluster.cu", "krylov_cluster1.cu", "batch.cu", "monitor.cu", "mesh.cu", "capi.cu"]
+SOURCES = ["fields.cu", "assemble.cu", "krylov.cu", "krylov_cluster.cu", "krylov_cluster1.cu", "batch.cu", "monitor.cu",
+           "mesh.cu", "terms.cu", "capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=default"]
 

@@ -421,6 +421,93 @@ int wcfd_replace_row(const wcfd_mesh* m, wcfd_system A, int32_t row, float value
     return WCFD_OK;
 }
 
+static int check_term_fields(const wcfd_term_fields& f) {
+    RET_IF(f.n < 1 || f.n > 3, WCFD_ERR_ARGUMENT, "a term acts on 1..3 fields");
+    for (int q = 0; q < f.n; ++q) RET_IF(f.index[q] < 0 || f.index[q] > 3, WCFD_ERR_ARGUMENT, "field index out of 0..3");
+    return WCFD_OK;
+}
+
+static int grid_slots(const wcfd_mesh* m) { return (m->n_cells * m->faces_per_cell + kBlock - 1) / kBlock; }
+
+int wcfd_convection_weights(const wcfd_mesh* m, wcfd_state s, wcfd_term_fields f, int32_t scheme, float* weights,
+                            void* stream) {
+    int rc = check_mesh(m);
+    if (rc) return rc;
+    rc = check_term_fields(f);
+    if (rc) return rc;
+    RET_IF(scheme < 0 || scheme > 2, WCFD_ERR_ARGUMENT, "convection scheme must be 0 upwind, 1 central, 2 upwindLinear");
+    RET_IF(!weights || !s.mass_fluxes || !s.face_values || !s.cell_gradients || !m->face_dvec, WCFD_ERR_ARGUMENT,
+           "null array");
+    convection_weights_kernel<<<grid_slots(m), kBlock, 0, S(stream)>>>(*m, s, f, scheme, weights);
+    LAUNCH_CHECK("convection_weights_kernel");
+    return WCFD_OK;
+}
+
+int wcfd_diffusion_weights(const wcfd_mesh* m, wcfd_bc bc, wcfd_state s, wcfd_term_fields f, float nu,
+                           const float* nu_faces, int32_t corrected, int32_t bc_mode, float bc_value, float* weights,
+                           void* stream) {
+    int rc = check_mesh(m);
+    if (rc) return rc;
+    rc = check_term_fields(f);
+    if (rc) return rc;
+    RET_IF(bc_mode != 0 && bc_mode != 1, WCFD_ERR_ARGUMENT, "bc_mode must be 0 (boundary table) or 1 (uniform gradient)");
+    RET_IF(!weights || !s.face_values || !s.face_gradients || !s.cell_gradients || !m->face_dvec ||
+           (bc_mode == 0 && !bc.type), WCFD_ERR_ARGUMENT, "null array");
+    diffusion_weights_kernel<<<grid_slots(m), kBlock, 0, S(stream)>>>(*m, bc, s, f, nu, nu_faces, corrected, bc_mode,
+                                                                       bc_value, weights);
+    LAUNCH_CHECK("diffusion_weights_kernel");
+    return WCFD_OK;
+}
+
+int wcfd_ddt_weights(const wcfd_mesh* m, wcfd_state s, wcfd_term_fields f, float dt, float* weights, void* stream) {
+    int rc = check_mesh(m);
+    if (rc) return rc;
+    rc = check_term_fields(f);
+    if (rc) return rc;
+    RET_IF(!(dt > 0.0f), WCFD_ERR_ARGUMENT, "dt must be positive");
+    RET_IF(!weights || !s.cell_values, WCFD_ERR_ARGUMENT, "null array");
+    ddt_weights_kernel<<<grid_for(m->n_cells * f.n), kBlock, 0, S(stream)>>>(*m, s, f, dt, weights);
+    LAUNCH_CHECK("ddt_weights_kernel");
+    return WCFD_OK;
+}
+
+int wcfd_grad_weights(const wcfd_mesh* m, wcfd_state s, int32_t field, float* weights, void* stream) {
+    int rc = check_mesh(m);
+    if (rc) return rc;
+    RET_IF(field < 0 || field > 3, WCFD_ERR_ARGUMENT, "field index out of 0..3");
+    RET_IF(!weights || !s.cell_gradients, WCFD_ERR_ARGUMENT, "null array");
+    grad_weights_kernel<<<grid_for(3 * m->n_cells), kBlock, 0, S(stream)>>>(*m, s, field, weights);
+    LAUNCH_CHECK("grad_weights_kernel");
+    return WCFD_OK;
+}
+
+int wcfd_assemble_terms(const wcfd_mesh* m, wcfd_system A, const wcfd_term* terms, int32_t n_terms, void* stream) {
+    int rc = check_mesh(m);
+    if (rc) return rc;
+    RET_IF(!A.diag || !A.off || !A.rhs || (A.ncomp != 1 && A.ncomp != 3), WCFD_ERR_ARGUMENT, "bad system");
+    RET_IF(n_terms < 0 || n_terms > WCFD_MAX_TERMS || (n_terms > 0 && !terms), WCFD_ERR_ARGUMENT,
+           "0..WCFD_MAX_TERMS terms");
+    TermList tl = {};
+    tl.count = n_terms;
+    for (int t = 0; t < n_terms; ++t) {
+        RET_IF(!terms[t].weights, WCFD_ERR_ARGUMENT, "a term without weights (call the term first)");
+        tl.weights[t] = terms[t].weights;
+        tl.scale[t] = terms[t].scale;
+        tl.cell_based[t] = terms[t].cell_based ? 1 : 0;
+    }
+    assemble_terms_kernel<<<grid_for(m->n_cells), kBlock, 0, S(stream)>>>(*m, A, tl);
+    LAUNCH_CHECK("assemble_terms_kernel");
+    return WCFD_OK;
+}
+
+int wcfd_add_rhs(float* rhs, const float* arr, float scale, int64_t n, void* stream) {
+    RET_IF(n < 0 || (n > 0 && (!rhs || !arr)), WCFD_ERR_ARGUMENT, "bad arrays");
+    if (n == 0) return WCFD_OK;
+    add_rhs_kernel<<<(unsigned)((n + kBlock - 1) / kBlock), kBlock, 0, S(stream)>>>(n, rhs, arr, scale);
+    LAUNCH_CHECK("add_rhs_kernel");
+    return WCFD_OK;
+}
+
 int wcfd_spmv(const wcfd_mesh* m, wcfd_system A, const float* x, float* y, void* stream) {
     int rc = check_mesh(m);
     if (rc) return rc;

@@ -29,6 +29,21 @@ void launch_pressure_assemble(bool xt, int grid, cudaStream_t st, const wcfd_mes
                               const wcfd_state& s, const wcfd_system& sys, const float* rua_faces, const float* div,
                               const wcfd_params& prm);
 
+// Term / Equation API (terms.cu)
+struct TermList {
+    int count;
+    float scale[WCFD_MAX_TERMS];
+    int cell_based[WCFD_MAX_TERMS];
+    const float* weights[WCFD_MAX_TERMS];
+};
+__global__ void convection_weights_kernel(wcfd_mesh m, wcfd_state s, wcfd_term_fields tf, int scheme, float* w);
+__global__ void diffusion_weights_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s, wcfd_term_fields tf, float nu,
+                                         const float* nu_faces, int corrected, int bc_mode, float bc_value, float* w);
+__global__ void ddt_weights_kernel(wcfd_mesh m, wcfd_state s, wcfd_term_fields tf, float dt, float* w);
+__global__ void grad_weights_kernel(wcfd_mesh m, wcfd_state s, int field, float* w);
+__global__ void assemble_terms_kernel(wcfd_mesh m, wcfd_system sys, TermList tl);
+__global__ void add_rhs_kernel(int64_t n, float* rhs, const float* a, float scale);
+
 // batched forms over a device case table (blockIdx.y = case)
 __global__ void face_pass_batched(const wcfd_case* cases, uint32_t mask, uint32_t flags);
 __global__ void face_pass_partial_batched(const wcfd_case* cases, uint32_t mask, uint32_t flags);
