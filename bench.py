@@ -387,7 +387,7 @@ def serve_mix(args, local, rank=0, world=1, dist=None):
     if dist is not None:
         dist.barrier()
     with ClockSampler(local, enabled=not args.no_clocks) as clocks:
-        rep = Server(max_outer=args.max_outer, max_active=args.max_active).run(reqs)
+        rep = Server(max_outer=args.max_outer, max_active=args.max_active, use_graphs=args.serve_graphs).run(reqs)
     summ = rep.summary()
     wall = max_over_ranks(summ["wall_s"])
     cell_its = sum_over_ranks(rep.cell_iterations)
@@ -398,9 +398,11 @@ def serve_mix(args, local, rank=0, world=1, dist=None):
     by_kind = {k: sum(r.kind == k for r in sample) for k in ("cavity", "channel")}
     mix_kind = {k: sum(r.kind == k for r in reqs) for k in ("cavity", "channel")}
     drop_status = {}
-    for _, _, r in drop["results"]:
+    for res in drop["results"]:
+        r = res[2]
         st = "converged" if r < 1e-6 else ("diverged" if not np.isfinite(r) else "exhausted")
         drop_status[st] = drop_status.get(st, 0) + 1
+    drop_status["retried"] = int(sum(res[3] > 0 for res in drop["results"]))
     return {
         "value": value, "wall": wall, "requests": len(reqs_all), "serving": summ, "clocks": clocks.summary(),
         "drop_in": {"requests_per_rank": len(sample), "sample": "stratified: evenly spaced over the mix sorted by "
@@ -623,6 +625,8 @@ def main():
     ap.add_argument("--rate", type=float, default=2000.0, help="serve workload: Poisson arrival rate (1/s)")
     ap.add_argument("--max-outer", type=int, default=4000, help="serve workload: outer-iteration cap per request")
     ap.add_argument("--drop-in-sample", type=int, default=48, help="serve workload: requests run through the drop-in")
+    ap.add_argument("--serve-graphs", type=int, default=0, help="serve workload: replay each bucket round as a "
+                    "captured CUDA graph (1) or launch it eagerly (0)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -139,3 +139,53 @@ def test_batch_with_explicit_terms_matches_alone():
     for _ in range(4):
         pb.step()
     assert not np.array_equal(fields(plain[0][0]), got[0])
+
+
+def test_batched_refined_pressure_equals_alone_and_tracks_drop_in():
+    """The batched form's fp64-refined pressure solve (two sweeps per corrector): a case in
+    the mix equals the same case alone (bitwise, same cluster size), and follows the
+    drop-in's refined solve (wcfd_cg_refine, the drop-in's own Krylov partition) within the
+    step tolerances."""
+    from warpcfd_gb300.batch import CaseBatch
+
+    def cases():
+        out = []
+        for mk, bc, ref, nu in ((lambda: cavity_mesh(16), cavity_bc, 0, 0.01),
+                                (lambda: channel_mesh(40, 8), channel_bc, None, 0.05),
+                                (lambda: cavity_mesh(24, jitter=0.1, seed=2), cavity_bc, 0, 0.005)):
+            model, solver, _ = make_pair(mk(), bc, ref_cell=ref, nu=nu, atol=1e-7)
+            solver.p_refine = 2
+            solver.p_refine_rtol = 1e-2
+            out.append((model, solver))
+        return out
+
+    steps = 4
+    mix = cases()
+    batch = CaseBatch([s for _, s in mix])
+    assert batch.dims.p_refine == 2
+    cs = batch.cluster_size
+    for _ in range(steps):
+        batch.step()
+    got = [fields(m) for m, _ in mix]
+    assert all(np.isfinite(g).all() for g in got)
+    for i, (model, solver) in enumerate(cases()):
+        alone = CaseBatch([solver], cluster_size=cs)
+        for _ in range(steps):
+            alone.step()
+        assert np.array_equal(fields(model), got[i]), i
+    for i, (model, solver) in enumerate(cases()):
+        for _ in range(steps):
+            solver.step()
+        ref = fields(model)
+        for o in range(3):
+            assert vel_err(got[i], ref, o) < 1e-4, (i, o)
+        assert rel_l2(got[i][:, 3], ref[:, 3]) < 1e-3, i
+
+
+def test_batch_rejects_mixed_refinement_counts():
+    from warpcfd_gb300.batch import CaseBatch
+
+    (m0, s0), (m1, s1) = [make_pair(cavity_mesh(8), cavity_bc)[:2] for _ in range(2)]
+    s1.p_refine = 1
+    with pytest.raises(ValueError, match="refinement"):
+        CaseBatch([s0, s1])

@@ -9,11 +9,15 @@ case through the C ABI in float32 with its solves tightened (momentum BiCGSTAB t
 1e-9, the pressure solve by fp64 iterative refinement).
 
 The bar per field (u, v, w on the velocity scale, p relative): within 1e-5 of the
-reference, or, where float32 arithmetic cannot get that close, within three times the
-distance of the oracle's own float32 run of the same method (same tightened solves, the
-reference's mesh arrays) from the reference.  Measured: on the cavities every field is
-within 2e-6; on the channel the float32 method itself is 1.4e-5 (u) and 8e-5 (p) away
-and the GPU the same; PISO p is 6e-5 (float32 oracle 3e-5).
+reference, or, where float32 arithmetic cannot get that close, within twice the float32
+floor of the method: the largest distance from the reference among the oracle's own
+float32 runs of the same method from the reference's mesh arrays, with the solves
+tightened in seven equally valid ways (pressure refinement of 2, 3, 4 or 6 sweeps, or the
+plain CG to atol 1e-8, 1e-9 or 1e-10).  Measured: on the cavities every field is within
+2e-6; on the channel the float32 method itself is 1.4e-5 (u) and 6-8e-5 (p) away and the
+GPU the same; on the PISO cavity the float32 variants put p 3e-6 to 5e-5 from the
+reference (p is small there, rms 0.008 against a velocity rms of 0.07, and taken without
+relaxation from the last corrector) and the GPU 6e-5.
 """
 import glob
 import os
@@ -61,11 +65,15 @@ def test_gpu_matches_the_reference(name):
     st = solver.solve_stats()
     assert st[0]["status"] == "ok" and st[1]["status"] == "ok", st
     e = field_errors(g, d["cell_values"])
-    # the float32 floor of the method: the oracle's float32 run with the same tightened
-    # solves (pressure refined the same way), from the reference's own mesh arrays
-    f32 = field_errors(oracle_run(d, T=np.float32, atol=1e-9, maxiter=5000, p_refine=4), d["cell_values"])
+    # the float32 floor of the method: the oracle's float32 runs with the solves tightened
+    # in equally valid ways, from the reference's own mesh arrays
+    variants = [dict(atol=1e-9, p_refine=r) for r in (2, 3, 4, 6)] + [dict(atol=a) for a in (1e-8, 1e-9, 1e-10)]
+    floor = {f: 0.0 for f in "uvwp"}
+    for kw in variants:
+        ev = field_errors(oracle_run(d, T=np.float32, maxiter=5000, **kw), d["cell_values"])
+        floor = {f: max(floor[f], ev[f]) for f in "uvwp"}
     fmt = lambda x: " ".join(f"{k} {v:.2e}" for k, v in x.items())  # noqa: E731
     print(f"\n{name}: GPU (fp32) vs the reference (fp64 on the Warp stand-in): {fmt(e)}"
-          f"\n{name}: fp32 oracle vs the reference: {fmt(f32)}")
+          f"\n{name}: float32 floor (largest fp32 oracle variant vs the reference): {fmt(floor)}")
     for f in "uvwp":
-        assert e[f] <= max(1e-5, 3.0 * f32[f]), (f, e, f32)
+        assert e[f] <= max(1e-5, 2.0 * floor[f]), (f, e, floor)

@@ -38,13 +38,16 @@ class CaseBatch:
             if (s.NUM_INNER_LOOPS, s.NUM_ORTHOGONAL_CORRECTORS) != (self.solvers[0].NUM_INNER_LOOPS,
                                                                       self.solvers[0].NUM_ORTHOGONAL_CORRECTORS):
                 raise ValueError("every case of a batch must use the same corrector counts")
+            if int(s.p_refine) != int(self.solvers[0].p_refine):
+                raise ValueError("every case of a batch must use the same number of pressure refinement sweeps")
         self.device = self.solvers[0].model.device
         n = len(self.solvers)
         self.stats = torch.zeros(n * 2 * _lib.STATS_BYTES, dtype=torch.uint8, device=self.device)
         self.dims = _lib.BatchDims_t(
             max(s.model.num_cells for s in self.solvers), max(s.model.num_faces for s in self.solvers),
             self.faces_per_cell, self.ell_width, self.solvers[0].NUM_INNER_LOOPS,
-            self.solvers[0].NUM_ORTHOGONAL_CORRECTORS, int(cluster_size), int(field_block))
+            self.solvers[0].NUM_ORTHOGONAL_CORRECTORS, int(cluster_size), int(field_block), 0,
+            int(self.solvers[0].p_refine))
         self._graph = None
         self._graph_steps = 0
         self.table = torch.empty(n * ct.sizeof(_lib.Case_t), dtype=torch.uint8, device=self.device)

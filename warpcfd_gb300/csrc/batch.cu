@@ -91,6 +91,32 @@ int launch_cluster(const void* fn, int n_cases, int cs, size_t smem, cudaStream_
     return WCFD_OK;
 }
 
+// One refinement sweep's residual for every case: r = b - A x64 with fp64 accumulation,
+// rounded once into p_work[0, C); the correction p_work[C, 2C) starts from zero.
+__global__ void __launch_bounds__(kMaxFieldBlock) refine_residual_batched(const wcfd_case* __restrict__ cases) {
+    const wcfd_case& c = cases[blockIdx.y];
+    const int C = c.mesh.n_cells;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= C) return;
+    const int W = c.mesh.ell_width;
+    double acc = (double)c.pres.diag[i] * c.p_x64[i];
+    for (int j = 0; j < W; ++j)
+        acc += (double)c.pres.off[(size_t)j * C + i] * c.p_x64[c.mesh.ell_col[(size_t)j * C + i]];
+    c.p_work[i] = (float)((double)c.pres.rhs[i] - acc);
+    c.p_work[C + i] = 0.0f;
+}
+
+// x64 += the sweep's correction; the field solution p_x is x64 rounded once
+__global__ void __launch_bounds__(kMaxFieldBlock) refine_update_batched(const wcfd_case* __restrict__ cases) {
+    const wcfd_case& c = cases[blockIdx.y];
+    const int C = c.mesh.n_cells;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= C) return;
+    const double v = c.p_x64[i] + (double)c.p_work[C + i];
+    c.p_x64[i] = v;
+    c.p_x[i] = (float)v;
+}
+
 #define BCHECK(what)                                                                               \
     do {                                                                                           \
         const cudaError_t e_ = cudaGetLastError();                                                 \
@@ -135,7 +161,8 @@ extern "C" int wcfd_batch_simple_iteration(const wcfd_case* cases, int32_t n_cas
     }
     const wcfd_batch_dims d = *dims;
     if (d.max_cells <= 0 || d.max_faces <= 0 || d.faces_per_cell < 1 || d.faces_per_cell > kMaxSlots ||
-        d.ell_width < 0 || d.ell_width > d.faces_per_cell || d.n_inner < 0 || d.n_ortho < 0 || n_cases > 65535) {
+        d.ell_width < 0 || d.ell_width > d.faces_per_cell || d.n_inner < 0 || d.n_ortho < 0 || n_cases > 65535 ||
+        d.p_refine < 0 || d.p_refine > 64) {
         std::snprintf(g_batch_error, sizeof(g_batch_error), "bad batch dims");
         return WCFD_ERR_ARGUMENT;
     }
@@ -186,9 +213,23 @@ extern "C" int wcfd_batch_simple_iteration(const wcfd_case* cases, int32_t n_cas
             BCHECK("gradient_batched");
             launch_assemble_batched(true, (d.explicit_terms & 4) != 0, gc, fb, st, cases);
             BCHECK("pressure_assemble_batched");
-            void* cargs[] = {(void*)&cases, &csv};
-            rc = launch_cluster(cg_fn, n_cases, cs, smem, st, cargs);
-            if (rc) return rc;
+            if (d.p_refine > 0) {
+                int one = 1;
+                for (int sw = 0; sw < d.p_refine; ++sw) {
+                    refine_residual_batched<<<gc, fb, 0, st>>>(cases);
+                    BCHECK("refine_residual_batched");
+                    void* cargs[] = {(void*)&cases, &csv, &one};
+                    rc = launch_cluster(cg_fn, n_cases, cs, smem, st, cargs);
+                    if (rc) return rc;
+                    refine_update_batched<<<gc, fb, 0, st>>>(cases);
+                    BCHECK("refine_update_batched");
+                }
+            } else {
+                int zero = 0;
+                void* cargs[] = {(void*)&cases, &csv, &zero};
+                rc = launch_cluster(cg_fn, n_cases, cs, smem, st, cargs);
+                if (rc) return rc;
+            }
             p_update_batched<<<gc, fb, 0, st>>>(cases);
             BCHECK("p_update_batched");
             face_pass_partial_batched<<<gf, fb, 0, st>>>(cases, WCFD_P, 0u);

@@ -245,9 +245,11 @@ __global__ void __launch_bounds__(CBS) cg_cluster_kernel(KrylovArgs a, int R) {
 }
 
 // One cluster per case of a device case table: the pressure CG of every case
-// (pres system, p_x warm start, stats[1]), cs CTAs per cluster.
+// (pres system, p_x warm start, stats[1]), cs CTAs per cluster.  refine = 1 solves a
+// refinement sweep's correction instead: right-hand side p_work[0, C) (the fp64 residual
+// rounded once), solution p_work[C, 2C) from zero, relative stop p_refine_rtol.
 template <int W, int RPT>
-__global__ void __launch_bounds__(CBS) cg_cluster_batched(const wcfd_case* __restrict__ cases, int cs) {
+__global__ void __launch_bounds__(CBS) cg_cluster_batched(const wcfd_case* __restrict__ cases, int cs, int refine) {
     const wcfd_case& c = cases[blockIdx.x / cs];
     KrylovArgs a = {};
     a.m = c.mesh;
@@ -255,6 +257,12 @@ __global__ void __launch_bounds__(CBS) cg_cluster_batched(const wcfd_case* __res
     a.x = c.p_x;
     a.atol2 = c.prm.atol_p * c.prm.atol_p;
     a.rtol2 = c.prm.rtol_p * c.prm.rtol_p;
+    if (refine) {
+        a.A.rhs = c.p_work;
+        a.x = c.p_work + c.mesh.n_cells;
+        a.atol2 = 0.0;
+        a.rtol2 = c.prm.p_refine_rtol * c.prm.p_refine_rtol;
+    }
     a.maxiter = c.prm.maxiter;
     a.stats = c.stats + 1;
     cg_cluster_body<W, RPT>(a, (c.mesh.n_cells + cs - 1) / cs);

@@ -58,6 +58,7 @@ class Result:
     finished: float
     fields: object = None
     rejected: str = ""   # why the request was never admitted ("" when it was)
+    retries: int = 0     # restarts at reduced relaxation after a divergence
 
     @property
     def latency(self):
@@ -131,11 +132,18 @@ RELAXATION = {
 # 3-4x the Krylov iterations (1e-10) for the same outer convergence.
 SERVE_ATOL = 1e-12
 SERVE_RTOL = (0.1, 0.1)
+# one fp64 refinement sweep of the pressure solve per outer iteration (its correction to the
+# same tenfold drop): the pressure of a converged case is accumulated in fp64
+SERVE_P_REFINE = 1
 
 
-def build_solver(req: Request, mesh, atol=1e-8, maxiter=500, device=None, rtol=(0.0, 0.0)):
-    """FVM + SIMPLE solver of one request (relaxation by kind, nu = speed * L / Re).
-    ``rtol`` = (momentum, pressure) relative Krylov stops on top of ``atol``."""
+def build_solver(req: Request, mesh, atol=1e-8, maxiter=500, device=None, rtol=(0.0, 0.0), relax_scale=1.0,
+                 p_refine=0):
+    """FVM + SIMPLE solver of one request (relaxation by kind times ``relax_scale``,
+    nu = speed * L / Re).  ``rtol`` = (momentum, pressure) relative Krylov stops on top of
+    ``atol``.  ``p_refine`` > 0: the pressure solve by that many fp64 refinement sweeps per
+    outer iteration, each correction solved to the pressure rtol (the precision form: p is
+    accumulated in fp64, so the converged pressure is not held at the fp32 CG's floor)."""
     nu = req.speed * 1.0 / req.re
     model = FVM(mesh, device=device)
     model.material.create_incompressible_newtonian_fluid(viscosity=nu, density=1.0)
@@ -154,13 +162,18 @@ def build_solver(req: Request, mesh, atol=1e-8, maxiter=500, device=None, rtol=(
     b.slip_wall("-Z")
     b.slip_wall("+Z")
     model.finalize()
-    solver = IncompressibleSolver(model, *RELAXATION[req.kind])
+    ur, pr = RELAXATION[req.kind]
+    solver = IncompressibleSolver(model, ur * relax_scale, pr * relax_scale)
     solver.verbose = False
     solver.vel_equation.tol = atol
     solver.p_corr_equation.tol = atol
     solver.vel_equation.rtol, solver.p_corr_equation.rtol = rtol
     solver.vel_equation.max_iter = maxiter
     solver.p_corr_equation.max_iter = maxiter
+    if p_refine > 0:
+        solver.p_refine = int(p_refine)
+        solver.p_refine_rtol = float(rtol[1]) if rtol[1] > 0 else 1e-3
+    solver.case_struct()   # allocates the refinement arrays now, so case_bytes counts them
     return model, solver
 
 
@@ -177,6 +190,7 @@ def case_bytes(model, solver, include_geometry=True) -> int:
           solver.vel_correction, solver.stats]
     if include_geometry:
         ts += [v for v in model._geo.values() if isinstance(v, torch.Tensor)]
+    ts += [t for t in (solver.p_x64, solver.p_work) if t is not None]
     for e in (solver.vel_equation, solver.p_corr_equation):
         ts += [e.diag, e.off, e.rhs, e.x, e.ws_vec, e.ws_partials, e.ws_results, e.ws_barrier, e.stats]
     return int(sum(t.numel() * t.element_size() for t in ts))
@@ -184,8 +198,9 @@ def case_bytes(model, solver, include_geometry=True) -> int:
 
 def estimate_bytes(cells: int) -> int:
     """Admission estimate before building: about 1.1 kB per cell for a 2D-extruded hex case
-    plus fixed workspaces (measured with case_bytes on the mix's meshes)."""
-    return int(1100 * cells + 2 * 8 * 2048 * 8 + 64 * 1024)
+    (16 B of it the fp64 pressure and refinement work arrays) plus fixed workspaces
+    (measured with case_bytes on the mix's meshes)."""
+    return int(1120 * cells + 2 * 8 * 2048 * 8 + 64 * 1024)
 
 
 def estimate_geometry_bytes(cells: int) -> int:
@@ -204,6 +219,7 @@ class _Slot:
     bytes: int
     admitted: float
     iterations: int = 0
+    retries: int = 0
 
 
 @dataclass
@@ -227,6 +243,8 @@ class ServeReport:
             "diverged": int(sum(r.status == "diverged" for r in self.results)),
             "exhausted": int(sum(r.status == "exhausted" for r in self.results)),
             "rejected": int(sum(r.status == "rejected" for r in self.results)),
+            "retried": int(sum(r.retries > 0 for r in self.results)),
+            "converged_after_retry": int(sum(r.retries > 0 and r.converged for r in self.results)),
             "p50_converged_s": float(np.percentile(lat_c, 50)),
             "p99_converged_s": float(np.percentile(lat_c, 99)),
             "p50_s": float(np.percentile(lat, 50)),
@@ -245,7 +263,8 @@ class Server:
 
     def __init__(self, hbm_budget=16 << 30, max_active=256, tol=1e-6, check_every=10, max_outer=4000,
                  buckets=(4096, 8192, 16384, 32768, 65536), atol=SERVE_ATOL, rtol=SERVE_RTOL, device=None,
-                 clock=time.perf_counter, keep_fields=False, autotune=True, use_graphs=False):
+                 clock=time.perf_counter, keep_fields=False, autotune=True, use_graphs=False, max_retries=1,
+                 retry_relax=0.5, p_refine=SERVE_P_REFINE):
         self.budget = int(hbm_budget)
         self.max_active = int(max_active)
         self.tol = float(tol)
@@ -259,6 +278,12 @@ class Server:
         self.meshes = MeshCache()
         self.autotune = autotune
         self.use_graphs = use_graphs
+        # divergence policy: a case whose residual turns non-finite starts again from zero
+        # fields with its relaxation factors scaled by retry_relax (per retry), at most
+        # max_retries times; the iterations before the restart stay counted
+        self.max_retries = int(max_retries)
+        self.retry_relax = float(retry_relax)
+        self.p_refine = int(p_refine)
         self._geometry_charged = set()
         self._geometry_bytes = 0
         self.keep_fields = keep_fields
@@ -326,13 +351,24 @@ class Server:
         """Build the case (the mesh and its device geometry come from caches) and charge its
         device bytes; a mesh's geometry is charged once, when it first reaches the device."""
         mesh = self.meshes.get(req.kind, req.cells)
-        model, solver = build_solver(req, mesh, atol=self.atol, device=self.device, rtol=self.rtol)
+        model, solver = build_solver(req, mesh, atol=self.atol, device=self.device, rtol=self.rtol,
+                                     p_refine=self.p_refine)
         nb = case_bytes(model, solver, include_geometry=False)
         key = self._mesh_key(req)
         if key not in self._geometry_charged:
             self._geometry_charged.add(key)
             self._geometry_bytes += geometry_bytes(model)
         return _Slot(req, model, solver, nb, self.clock() - t0)
+
+    def _restart(self, slot, t0):
+        """A fresh case for ``slot``'s request (zero fields) at its relaxation times
+        retry_relax ** (retries + 1); admission time and iterations carry over."""
+        mesh = self.meshes.get(slot.req.kind, slot.req.cells)
+        retries = slot.retries + 1
+        model, solver = build_solver(slot.req, mesh, atol=self.atol, device=self.device, rtol=self.rtol,
+                                     relax_scale=self.retry_relax ** retries, p_refine=self.p_refine)
+        nb = case_bytes(model, solver, include_geometry=False)
+        return _Slot(slot.req, model, solver, nb, slot.admitted, slot.iterations, retries)
 
     def run(self, requests) -> ServeReport:
         """Serve ``requests`` (arrival times relative to the start of the call).
@@ -416,11 +452,19 @@ class Server:
                         s.iterations += self.check_every
                         report.cell_iterations += s.model.num_cells * self.check_every
                         done = bool(r < self.tol)
+                        if (not math.isfinite(r) and s.retries < self.max_retries
+                                and s.iterations < self.max_outer):
+                            # diverged: restart from zero fields at reduced relaxation
+                            s2 = self._restart(s, t0)
+                            used += s2.bytes - s.bytes
+                            incoming[bi].append(s2)
+                            continue
                         if done or not math.isfinite(r) or s.iterations >= self.max_outer:
                             report.results.append(Result(s.req.rid, s.req.kind, s.model.num_cells, s.iterations,
                                                          done, float(r), s.req.arrival, s.admitted,
                                                          self.clock() - t0,
-                                                         s.model.cell_values.clone() if self.keep_fields else None))
+                                                         s.model.cell_values.clone() if self.keep_fields else None,
+                                                         retries=s.retries))
                             used -= s.bytes
                         else:
                             keep.append(s)
@@ -470,27 +514,39 @@ class Server:
         return report
 
 
-def run_drop_in(requests, tol=1e-6, check_every=10, max_outer=4000, atol=SERVE_ATOL, rtol=SERVE_RTOL, device=None):
+def run_drop_in(requests, tol=1e-6, check_every=10, max_outer=4000, atol=SERVE_ATOL, rtol=SERVE_RTOL, device=None,
+                max_retries=1, retry_relax=0.5, p_refine=SERVE_P_REFINE):
     """The same requests through the plain drop-in path, one case at a time in arrival
-    order: the baseline the batched server is compared with."""
+    order, with the server's stop and divergence policy (a diverged case restarts from
+    zero fields at reduced relaxation, at most ``max_retries`` times): the baseline the
+    batched server is compared with."""
     meshes = MeshCache()
     cell_iters = 0
     t0 = time.perf_counter()
     results = []
     for req in sorted(requests, key=lambda r: r.arrival):
-        model, solver = build_solver(req, meshes.get(req.kind, req.cells), atol=atol, device=device, rtol=rtol)
-        it = 0
+        mesh = meshes.get(req.kind, req.cells)
+        model, solver = build_solver(req, mesh, atol=atol, device=device, rtol=rtol, p_refine=p_refine)
+        total = 0
+        retries = 0
         r = float("inf")
-        while it < max_outer:
+        while total < max_outer:
             for _ in range(check_every):
                 solver.step()
-            it += check_every
+            total += check_every
+            cell_iters += model.num_cells * check_every
             st = solver.solve_stats()[0]
             r = st["initial_residual"] / max(st["rhs_norm"], 1e-300)
-            if r < tol or not math.isfinite(r):
+            if r < tol:
                 break
-        cell_iters += model.num_cells * it
-        results.append((req.rid, it, r))
+            if not math.isfinite(r):
+                if retries < max_retries and total < max_outer:
+                    retries += 1
+                    model, solver = build_solver(req, mesh, atol=atol, device=device, rtol=rtol,
+                                                 relax_scale=retry_relax ** retries, p_refine=p_refine)
+                    continue
+                break
+        results.append((req.rid, total, r, retries))
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     return {"cell_iterations_per_s": cell_iters / wall, "wall_s": wall, "results": results}
