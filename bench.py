@@ -43,7 +43,8 @@ WORKLOADS = {
                 "2 correctors and non-orthogonal correction, fp32 with fp64 iterative refinement of the pressure "
                 "solve (3 sweeps, inner relative stop 1e-3); one step = one time step",
     "serve": "serving mix: steady cavity/channel requests, cells log-uniform in [32^2, 256^2], Re ~ U[50, 1000], "
-             "speed ~ U[0.5, 2], seeded Poisson arrivals, converged to a 1e-6 relative momentum residual; "
+             "speed ~ U[0.5, 2], seeded Poisson arrivals, converged: relative momentum residual below 1e-6 and "
+             "no longer falling (no new minimum over 5 checks of 10 iterations); "
              "continuous batching (batched form) vs the drop-in path one case at a time",
 }
 METRIC = "cell-iterations/s"
@@ -387,7 +388,8 @@ def serve_mix(args, local, rank=0, world=1, dist=None):
     if dist is not None:
         dist.barrier()
     with ClockSampler(local, enabled=not args.no_clocks) as clocks:
-        rep = Server(max_outer=args.max_outer, max_active=args.max_active, use_graphs=args.serve_graphs).run(reqs)
+        rep = Server(max_outer=args.max_outer, max_active=args.max_active, use_graphs=args.serve_graphs,
+                     admission=args.admission).run(reqs)
     summ = rep.summary()
     wall = max_over_ranks(summ["wall_s"])
     cell_its = sum_over_ranks(rep.cell_iterations)
@@ -400,7 +402,7 @@ def serve_mix(args, local, rank=0, world=1, dist=None):
     drop_status = {}
     for res in drop["results"]:
         r = res[2]
-        st = "converged" if r < 1e-6 else ("diverged" if not np.isfinite(r) else "exhausted")
+        st = "converged" if res[4] else ("diverged" if not np.isfinite(r) else "exhausted")
         drop_status[st] = drop_status.get(st, 0) + 1
     drop_status["retried"] = int(sum(res[3] > 0 for res in drop["results"]))
     return {
@@ -625,7 +627,9 @@ def main():
     ap.add_argument("--rate", type=float, default=2000.0, help="serve workload: Poisson arrival rate (1/s)")
     ap.add_argument("--max-outer", type=int, default=4000, help="serve workload: outer-iteration cap per request")
     ap.add_argument("--drop-in-sample", type=int, default=48, help="serve workload: requests run through the drop-in")
-    ap.add_argument("--serve-graphs", type=int, default=0, help="serve workload: replay each bucket round as a "
+    ap.add_argument("--admission", default="fifo", choices=["fifo", "largest"],
+                    help="serve workload: admission order of arrived requests")
+    ap.add_argument("--serve-graphs", type=int, default=1, help="serve workload: replay each bucket round as a "
                     "captured CUDA graph (1) or launch it eagerly (0)")
     args = ap.parse_args()
     if args.warmup < 3:

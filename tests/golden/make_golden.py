@@ -26,6 +26,20 @@ ldc64_fp64_500_refined.npz, channel400_fp64_100_refined.npz : fp64 fields, momen
 The channel fixtures store cell_values as float32 to keep the files small (the rounding,
 6e-8 relative, is far below the distances they are compared at).
 Each file stores cell_values (C,4) and the per-iteration Krylov counts.
+
+serve_fp64_converged.npz : three requests of the serving mix's mesh ladder (a 32 x 32 cavity
+                           at Re 100 and speed 1, a 51 x 51 cavity at Re 400 and speed 1.5, a
+                           128 x 32 channel on 4 x 1 at Re 100 and speed 1), each run by the
+                           fp64 oracle at the server's relaxation (0.7 / 0.3 cavity, 0.3 / 0.3
+                           channel), momentum atol 1e-13 and the pressure solved by 4 fp64
+                           refinement sweeps per iteration (an absolute stop alone leaves the
+                           pinned pressure system's solution moving at ~1e-6), until no field
+                           moves by more than 1e-10 of its scale over an iteration (five orders
+                           below the 1e-5 the served results are held to): the fixed point a
+                           served result is compared with.  r{i}_fp32 holds the fp32 oracle's run
+                           of the same request (momentum atol 1e-9, the same pressure refinement)
+                           for as many iterations as the fp64 run took plus half: the fp32 floor
+                           of the method against that fixed point.
 """
 import os
 import sys
@@ -63,7 +77,54 @@ def case_for(spec):
     return m, host_boundary(m, channel_bc), 1.0 / 200.0, None, (0.3, 0.3)
 
 
+SERVE_REQUESTS = [  # (rid, kind, cells, Re, speed)
+    (0, "cavity", 1024, 100.0, 1.0),
+    (1, "cavity", 2500, 400.0, 1.5),
+    (2, "channel", 4096, 100.0, 1.0),
+]
+
+
+def make_serve_converged(max_iters=8000):
+    from warpcfd_gb300.serve import RELAXATION, MeshCache
+
+    mc = MeshCache()
+    out = {}
+    for rid, kind, cells, re, speed in SERVE_REQUESTS:
+        m = mc.get(kind, cells)
+        nu = speed / re
+        if kind == "cavity":
+            b = host_boundary(m, cavity_bc, lid=speed)
+            ref = 0
+        else:
+            b = host_boundary(m, channel_bc, u_in=speed)
+            ref = None
+        oc = OracleCase(geometry_from_mesh(m), b.boundary_type, b.boundary_values, nu, 1.0, T=np.float64,
+                        reference_cell=ref, atol=1e-13, maxiter=20000, p_refine=4, p_refine_rtol=1e-3)
+        ur, pr = RELAXATION[kind]
+        t = time.time()
+        for it in range(max_iters):
+            prev = oc.cell_values.copy()
+            oc.run(ur, pr, n_outer=1)
+            scale = np.abs(oc.cell_values).max(axis=0) + 1e-300
+            if np.all(np.abs(oc.cell_values - prev).max(axis=0) <= 1e-10 * scale):
+                break
+        else:
+            raise RuntimeError(f"request {rid} did not reach its fixed point in {max_iters} iterations")
+        print(f"serve request {rid} ({kind}, {m.num_cells} cells): {it + 1} iterations, {time.time() - t:.1f}s",
+              flush=True)
+        out[f"r{rid}"] = oc.cell_values.copy()
+        out[f"r{rid}_spec"] = np.array([rid, cells, re, speed, 1.0 if kind == "cavity" else 0.0])
+        out[f"r{rid}_iterations"] = it + 1
+        o32 = OracleCase(geometry_from_mesh(m), b.boundary_type, b.boundary_values, nu, 1.0, T=np.float32,
+                         reference_cell=ref, atol=1e-9, maxiter=20000, p_refine=4, p_refine_rtol=1e-3)
+        o32.run(ur, pr, n_outer=(3 * (it + 1)) // 2)
+        out[f"r{rid}_fp32"] = o32.cell_values.astype(np.float64)
+    np.savez_compressed(os.path.join(HERE, "serve_fp64_converged.npz"), **out)
+
+
 def make(name):
+    if name == "serve_fp64_converged":
+        return make_serve_converged()
     spec = SPECS[name]
     m, b, nu, ref, relax = case_for(spec)
     oc = OracleCase(geometry_from_mesh(m), b.boundary_type, b.boundary_values, nu, 1.0, T=spec["T"],
@@ -79,7 +140,7 @@ def make(name):
 
 
 if __name__ == "__main__":
-    names = sys.argv[1:] or list(SPECS)
+    names = sys.argv[1:] or (list(SPECS) + ["serve_fp64_converged"])
     if len(names) > 1:
         import multiprocessing as mp
 

@@ -57,3 +57,24 @@ def test_server_rejects_what_it_can_never_serve():
     small = Server(hbm_budget=1 << 20, max_outer=20, autotune=False).run([Request(0, "cavity", 32 * 32, 100.0, 1.0, 0.0)])
     assert [r.status for r in small.results] == ["rejected"]
     assert "budget" in small.results[0].rejected
+
+
+def test_admission_order_does_not_change_results():
+    """Longest-first admission (admission='largest') changes when a request runs, not what it
+    computes: every result equals the first-come-first-served run's, bit for bit, and the
+    diverged-request policy (a restart at half relaxation) is counted in the summary."""
+    from warpcfd_gb300.serve import Server, make_request_mix
+
+    reqs = make_request_mix(10, seed=11, rate=5000.0, lo=32 * 32, hi=64 * 64)
+    kw = dict(tol=1e-4, check_every=10, max_outer=200, buckets=(1024, 4096), keep_fields=True, atol=1e-7,
+              max_active=4)
+    fifo = {r.rid: r for r in Server(**kw).run(reqs).results}
+    rep = Server(admission="largest", **kw).run(reqs)
+    largest = {r.rid: r for r in rep.results}
+    assert set(fifo) == set(largest) == {r.rid for r in reqs}
+    for rid, a in fifo.items():
+        b = largest[rid]
+        assert (a.iterations, a.status, a.retries) == (b.iterations, b.status, b.retries)
+        assert torch.equal(a.fields.view(torch.int32), b.fields.view(torch.int32))
+    s = rep.summary()
+    assert "retried" in s and "converged_after_retry" in s

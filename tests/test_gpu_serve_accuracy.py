@@ -1,0 +1,58 @@
+"""Served results against the fp64 oracle's converged solution.
+
+Three requests of the serving mix's mesh ladder (a 32 x 32 cavity at Re 100, a 51 x 51
+cavity at Re 400 with lid speed 1.5, a 128 x 32 channel at Re 100) are served to the
+server's own stop (relative momentum residual below 1e-6 and no longer falling, Krylov
+solves to a tenfold drop, the pressure accumulated in fp64 by one refinement sweep per
+outer iteration) and each served field is compared with the fp64 oracle's fixed point of
+the same case (tests/golden/make_golden.py serve_fp64_converged): u, v, w on the velocity
+scale and p relative, within 1e-5 -- or, where float32 arithmetic cannot get that close,
+within three times the fp32 oracle's own distance from that fixed point (the fixture's
+r{i}_fp32; measured: the channel's p, ~2e-5).
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib_ready():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from warpcfd_gb300.build import build_library
+    build_library()
+
+
+def test_served_results_match_the_fp64_oracle():
+    from warpcfd_gb300.serve import Request, Server
+
+    fx = np.load(os.path.join(GOLDEN, "serve_fp64_converged.npz"))
+    reqs = []
+    for key in sorted(k for k in fx.files if k.endswith("_spec")):
+        rid, cells, re, speed, is_cavity = fx[key]
+        reqs.append(Request(int(rid), "cavity" if is_cavity else "channel", int(cells), float(re), float(speed), 0.0))
+    rep = Server(keep_fields=True, max_outer=8000).run(reqs)
+    assert len(rep.results) == len(reqs)
+    errs = {}
+    for r in sorted(rep.results, key=lambda r: r.rid):
+        assert r.status == "converged", (r.rid, r.status, r.iterations, r.residual)
+        got = r.fields.double().cpu().numpy()
+        ref = fx[f"r{r.rid}"]
+        un = np.linalg.norm(ref[:, 0:3])
+        e = {f: float(np.linalg.norm(got[:, i] - ref[:, i]) / un) for i, f in enumerate("uvw")}
+        e["p"] = float(np.linalg.norm(got[:, 3] - ref[:, 3]) / np.linalg.norm(ref[:, 3]))
+        f32 = fx[f"r{r.rid}_fp32"]
+        floor = {f: float(np.linalg.norm(f32[:, i] - ref[:, i]) / un) for i, f in enumerate("uvw")}
+        floor["p"] = float(np.linalg.norm(f32[:, 3] - ref[:, 3]) / np.linalg.norm(ref[:, 3]))
+        fmt = lambda x: " ".join(f"{k} {v:.2e}" for k, v in x.items())  # noqa: E731
+        print(f"\nserved request {r.rid} ({r.kind}, {r.cells} cells, {r.iterations} iterations) vs the fp64 "
+              f"oracle's fixed point: {fmt(e)}; fp32 oracle vs the fixed point: {fmt(floor)}")
+        errs[r.rid] = (e, floor)
+    for rid, (e, floor) in errs.items():
+        for f in "uvwp":
+            assert e[f] <= max(1e-5, 3.0 * floor[f]), (rid, f, e, floor)

@@ -5,7 +5,7 @@ import math
 import numpy as np
 
 from warpcfd_gb300.serve import (CHANNEL_ASPECT, RELAXATION, MeshCache, Request, Result, Server, ServeReport,
-                                 estimate_bytes, estimate_geometry_bytes, make_request_mix, side_ladder)
+                                 StopRule, estimate_bytes, estimate_geometry_bytes, make_request_mix, side_ladder)
 
 
 def test_request_mix_is_seeded_and_within_bounds():
@@ -129,3 +129,18 @@ def test_rejected_results_are_counted_and_kept_out_of_latency():
     summary = rep.summary()
     assert summary["requests"] == 2 and summary["rejected"] == 1 and summary["converged"] == 1
     assert summary["p50_s"] == summary["p99_s"] == 2.0
+
+
+def test_stop_rule_waits_for_the_residual_floor():
+    """Converged = below tol and no new residual minimum for `patience` checks."""
+    rule = StopRule(1e-6, patience=3)
+    st = [float("inf"), 0]
+    seq = [1e-3, 1e-5, 9e-7, 5e-7, 3e-7, 2e-7, 2.1e-7, 1.9999e-7, 2.05e-7]
+    out = [rule.update(st, r) for r in seq]
+    # falling below tol is not enough; three checks without a new minimum (0.1% better) are
+    assert out == [False] * 8 + [True]
+    assert StopRule(1e-6, patience=0).update([float("inf"), 0], 5e-7)
+    assert not StopRule(1e-6, patience=0).update([float("inf"), 0], 2e-6)
+    # a restart (new state) starts counting afresh
+    st2 = [float("inf"), 0]
+    assert not rule.update(st2, 2e-7)

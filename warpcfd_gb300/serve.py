@@ -211,6 +211,27 @@ def estimate_geometry_bytes(cells: int) -> int:
     return int(420 * cells + 64 * 1024)
 
 
+class StopRule:
+    """When a steady case counts as converged: its relative momentum residual (the initial
+    residual of the outer iteration's momentum solve over ||b||) is below ``tol`` AND has
+    stopped falling -- no new minimum (by more than 0.1%) over the last ``patience`` checks.
+    The residual of an fp32 solve floors at ~1e-7 (~6e-8 on channels); a case stopped at
+    1e-6 alone is still 3e-5 to 2e-4 from the fp64 fixed point, one run to its floor is
+    within ~1e-6 on the velocities and ~1e-5 on p.  patience = 0 stops at ``tol``."""
+
+    def __init__(self, tol=1e-6, patience=5):
+        self.tol = float(tol)
+        self.patience = int(patience)
+
+    def update(self, state, r) -> bool:
+        """``state`` is the case's [best residual, checks since it]; True when converged."""
+        if r < state[0] * (1.0 - 1e-3):
+            state[0], state[1] = r, 0
+        else:
+            state[1] += 1
+        return bool(r < self.tol) and (self.patience == 0 or state[1] >= self.patience)
+
+
 @dataclass
 class _Slot:
     req: Request
@@ -220,6 +241,7 @@ class _Slot:
     admitted: float
     iterations: int = 0
     retries: int = 0
+    stop_state: list = field(default_factory=lambda: [float("inf"), 0])
 
 
 @dataclass
@@ -261,13 +283,14 @@ class ServeReport:
 class Server:
     """Continuous batching over size buckets (bucket = cell count up to its bound)."""
 
-    def __init__(self, hbm_budget=16 << 30, max_active=256, tol=1e-6, check_every=10, max_outer=4000,
+    def __init__(self, hbm_budget=16 << 30, max_active=256, tol=1e-6, check_every=10, max_outer=4000, patience=5,
                  buckets=(4096, 8192, 16384, 32768, 65536), atol=SERVE_ATOL, rtol=SERVE_RTOL, device=None,
-                 clock=time.perf_counter, keep_fields=False, autotune=True, use_graphs=False, max_retries=1,
-                 retry_relax=0.5, p_refine=SERVE_P_REFINE):
+                 clock=time.perf_counter, keep_fields=False, autotune=True, use_graphs=True, max_retries=1,
+                 retry_relax=0.5, p_refine=SERVE_P_REFINE, admission="fifo"):
         self.budget = int(hbm_budget)
         self.max_active = int(max_active)
         self.tol = float(tol)
+        self.stop = StopRule(tol, patience)
         self.check_every = int(check_every)
         self.max_outer = int(max_outer)
         self.bounds = tuple(sorted(buckets))
@@ -284,6 +307,11 @@ class Server:
         self.max_retries = int(max_retries)
         self.retry_relax = float(retry_relax)
         self.p_refine = int(p_refine)
+        # order in which arrived requests are admitted: "fifo" (arrival order) or "largest"
+        # (most cells first, arrival order among equals)
+        if admission not in ("fifo", "largest"):
+            raise ValueError("admission must be 'fifo' or 'largest'")
+        self.admission = admission
         self._geometry_charged = set()
         self._geometry_bytes = 0
         self.keep_fields = keep_fields
@@ -394,18 +422,27 @@ class Server:
         cur = torch.cuda.current_stream(self.device)
         t0 = self.clock()
         qi = 0
-        while qi < len(pending) or any(active) or any(incoming):
+        waiting = []                         # arrived, not yet admitted, in admission order
+        while qi < len(pending) or waiting or any(active) or any(incoming):
             # admission: arrived requests while slots and memory allow
             now = self.clock() - t0
+            arrived = False
             while qi < len(pending) and pending[qi].arrival <= now:
-                req = pending[qi]
+                waiting.append(pending[qi])
+                qi += 1
+                arrived = True
+            if arrived and self.admission == "largest":
+                # longest first: the large cases start early and small ones fill the tail
+                waiting.sort(key=lambda r: (-r.cells, r.arrival))
+            while waiting:
+                req = waiting[0]
                 # a request that no state of the server can admit is rejected, not queued
                 # (it would hold the head of the queue for ever)
                 why = self._never_admissible(req)
                 if why:
                     report.results.append(Result(req.rid, req.kind, req.cells, 0, False, float("nan"), req.arrival,
                                                  now, now, None, why))
-                    qi += 1
+                    waiting.pop(0)
                     continue
                 n_live = sum(len(a) for a in active) + sum(len(a) for a in incoming)
                 if n_live >= self.max_active or not self._fits(req, used):
@@ -417,7 +454,7 @@ class Server:
                     report.admit_s += self.clock() - ta
                     report.results.append(Result(req.rid, req.kind, req.cells, 0, False, float("nan"), req.arrival,
                                                  now, self.clock() - t0, None, f"cannot build the case: {e}"))
-                    qi += 1
+                    waiting.pop(0)
                     continue
                 report.admit_s += self.clock() - ta
                 if used + slot.bytes + self._geometry_bytes > self.budget:
@@ -429,13 +466,13 @@ class Server:
                         report.results.append(Result(req.rid, req.kind, req.cells, 0, False, float("nan"),
                                                      req.arrival, now, self.clock() - t0, None,
                                                      "measured device bytes exceed the budget"))
-                        qi += 1
+                        waiting.pop(0)
                         continue
                     break
                 used += slot.bytes
                 report.peak_bytes = max(report.peak_bytes, used + self._geometry_bytes)
                 incoming[self._bucket(slot.model.num_cells)].append(slot)
-                qi += 1
+                waiting.pop(0)
             report.max_active = max(report.max_active, sum(len(a) for a in active) + sum(len(a) for a in incoming))
             progressed = False
             for bi in range(nb):
@@ -451,7 +488,7 @@ class Server:
                     for s, r in zip(active[bi], res):
                         s.iterations += self.check_every
                         report.cell_iterations += s.model.num_cells * self.check_every
-                        done = bool(r < self.tol)
+                        done = self.stop.update(s.stop_state, r)
                         if (not math.isfinite(r) and s.retries < self.max_retries
                                 and s.iterations < self.max_outer):
                             # diverged: restart from zero fields at reduced relaxation
@@ -504,7 +541,7 @@ class Server:
                 inflight[bi] = (e0, e1, host)
                 progressed = True
             if not progressed:
-                if not any(active) and not any(incoming) and qi < len(pending):
+                if not any(active) and not any(incoming) and not waiting and qi < len(pending):
                     time.sleep(max(0.0, min(pending[qi].arrival - (self.clock() - t0), 0.01)))
                 else:
                     time.sleep(20e-6)
@@ -515,12 +552,13 @@ class Server:
 
 
 def run_drop_in(requests, tol=1e-6, check_every=10, max_outer=4000, atol=SERVE_ATOL, rtol=SERVE_RTOL, device=None,
-                max_retries=1, retry_relax=0.5, p_refine=SERVE_P_REFINE):
+                max_retries=1, retry_relax=0.5, p_refine=SERVE_P_REFINE, patience=5):
     """The same requests through the plain drop-in path, one case at a time in arrival
     order, with the server's stop and divergence policy (a diverged case restarts from
     zero fields at reduced relaxation, at most ``max_retries`` times): the baseline the
     batched server is compared with."""
     meshes = MeshCache()
+    stop = StopRule(tol, patience)
     cell_iters = 0
     t0 = time.perf_counter()
     results = []
@@ -530,6 +568,7 @@ def run_drop_in(requests, tol=1e-6, check_every=10, max_outer=4000, atol=SERVE_A
         total = 0
         retries = 0
         r = float("inf")
+        state = [float("inf"), 0]
         while total < max_outer:
             for _ in range(check_every):
                 solver.step()
@@ -537,16 +576,18 @@ def run_drop_in(requests, tol=1e-6, check_every=10, max_outer=4000, atol=SERVE_A
             cell_iters += model.num_cells * check_every
             st = solver.solve_stats()[0]
             r = st["initial_residual"] / max(st["rhs_norm"], 1e-300)
-            if r < tol:
-                break
             if not math.isfinite(r):
                 if retries < max_retries and total < max_outer:
                     retries += 1
                     model, solver = build_solver(req, mesh, atol=atol, device=device, rtol=rtol,
                                                  relax_scale=retry_relax ** retries, p_refine=p_refine)
+                    state = [float("inf"), 0]
                     continue
                 break
-        results.append((req.rid, total, r, retries))
+            if stop.update(state, r):
+                break
+        converged = bool(math.isfinite(r) and r < tol and (patience == 0 or state[1] >= patience))
+        results.append((req.rid, total, r, retries, converged))
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     return {"cell_iterations_per_s": cell_iters / wall, "wall_s": wall, "results": results}
