@@ -43,3 +43,22 @@ def test_per_face_values_follow_the_group_order():
     # rows in boundary order, values assigned to them in that order
     assert np.array_equal(b.boundary_values[rows, 0], vals)
     assert np.all(b.boundary_type[rows, 0] == 1)
+
+
+def test_boundary_rows_lookup_equals_set_membership():
+    """The face-id lookup set_value uses gives the rows np.where(np.isin(boundary_ids,
+    face_ids)) gives (boundary.py:40-45), duplicates and non-boundary ids included."""
+    import numpy as np
+
+    from warpcfd_gb300.FV.boundary.boundary import Boundary
+
+    rng = np.random.default_rng(0)
+    for t in range(100):
+        bids = np.sort(rng.choice(5000, size=rng.integers(1, 800), replace=False)).astype(np.int32)
+        b = Boundary({"u": None}, {}, bids)
+        f = rng.choice(bids, size=rng.integers(1, 300))
+        if t % 3 == 0:
+            f = np.concatenate([f, rng.integers(-3, 6000, size=5)])
+        rows, ok = b._rows(f)
+        assert np.array_equal(rows, np.where(np.isin(bids, f))[0])
+        assert ok == bool(np.all(np.isin(f, bids)))

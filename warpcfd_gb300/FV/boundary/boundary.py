@@ -26,17 +26,35 @@ class Boundary:
         self.float_dtype = float_type
         self._boundary_types = {"dirichlet": DIRICHLET, "vonNeumann": NEUMANN}
         self.finalized = False
+        self._row_of = None   # face id -> boundary row (-1: not a boundary face), built on first use
+
+    def _rows(self, face_ids):
+        """(rows, all_boundary): the boundary rows of ``face_ids`` in boundary order, each
+        once -- the rows np.where(np.isin(boundary_ids, face_ids)) gives -- and whether every
+        id is a boundary face, by a face-id lookup table instead of sorted set membership."""
+        B = len(self.boundary_ids)
+        if self._row_of is None:
+            bids = self.boundary_ids.astype(np.int64)
+            self._row_of = np.full(int(bids.max()) + 1 if B else 0, -1, dtype=np.int64)
+            self._row_of[bids] = np.arange(B)
+        f = np.asarray(face_ids).astype(np.int64, copy=False).reshape(-1)
+        inside = (f >= 0) & (f < self._row_of.shape[0])
+        r = self._row_of[f[inside]]
+        all_boundary = bool(inside.all()) and bool((r >= 0).all())
+        mask = np.zeros(B, dtype=bool)
+        mask[r[r >= 0]] = True
+        return np.flatnonzero(mask), all_boundary
 
     def set_value(self, face_ids, boundary_type="dirchlet", **output_vars):
         face_ids = self.get_face_id_array(face_ids)
-        if not np.all(np.isin(face_ids, self.boundary_ids)):
+        rows, all_boundary = self._rows(face_ids)
+        if not all_boundary:
             raise AssertionError("One or more of the provided face id is not an external face valid for "
                                  "applying boundary conditions")
         if not output_vars:
             raise AssertionError("You must specify some sort of output variable")
-        # rows in boundary order; a per-face array is assigned to them in that order,
-        # as boundary.py:320-324 does
-        rows = np.where(np.isin(self.boundary_ids, face_ids))[0]
+        # rows in boundary order; a per-face array is assigned to them in that order, as
+        # boundary.py:40-45 does (np.where(np.isin(self.boundary_ids, face_ids)))
         for output_name, value in output_vars.items():
             output = self.fields[output_name]
             self.boundary_values[rows, output.index] = np.asarray(value, dtype=np.float64)
