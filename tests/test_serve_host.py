@@ -144,3 +144,31 @@ def test_stop_rule_waits_for_the_residual_floor():
     # a restart (new state) starts counting afresh
     st2 = [float("inf"), 0]
     assert not rule.update(st2, 2e-7)
+
+
+def test_boundary_template_times_speed_equals_the_api_table():
+    """build_solver forms a kind's boundary table once per mesh at unit speed and scales it:
+    the same table, bit for bit, as the boundary helpers called at the request's speed."""
+    from warpcfd_gb300.FV.boundary.boundary import Boundary
+    from warpcfd_gb300.FV.field import Field
+
+    fields = {k: Field(k, i) for i, k in enumerate("uvwp")}
+    mc = MeshCache()
+
+    def table(m, kind, speed):
+        b = Boundary(fields, m.groups, m.face_properties.boundary_face_ids)
+        if kind == "cavity":
+            b.no_slip_wall("-X"), b.no_slip_wall("+X"), b.no_slip_wall("-Y")
+            b.velocity_BC("+Y", u=speed, v=0.0, w=0.0)
+        else:
+            b.velocity_BC("-X", u=speed, v=0.0, w=0.0), b.pressure_BC("+X", p=0.0)
+            b.no_slip_wall("-Y"), b.no_slip_wall("+Y")
+        b.slip_wall("-Z"), b.slip_wall("+Z")
+        return b.boundary_type, b.boundary_values
+
+    for kind, speed in (("cavity", 1.37), ("channel", 0.61), ("cavity", 2.0)):
+        m = mc.get(kind, 3000)
+        t1, v1 = table(m, kind, 1.0)
+        ts, vs = table(m, kind, speed)
+        assert np.array_equal(t1, ts)
+        assert np.array_equal((v1 * speed).view(np.int64), vs.view(np.int64))

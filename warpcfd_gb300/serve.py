@@ -95,9 +95,15 @@ def make_request_mix(n_requests=1024, seed=0, rate=200.0, lo=32 * 32, hi=256 * 2
 
 
 class MeshCache:
-    def __init__(self):
+    """Meshes of the size ladder, built on first use and kept.  With a CUDA ``device`` a
+    mesh is preprocessed by the GPU mesh pass (topology and fp64 geometry bit-identical to
+    the host pass; a 65,536-cell mesh in milliseconds instead of ~0.5 s of host time, which
+    would otherwise stall the serving loop that launches every bucket's rounds)."""
+
+    def __init__(self, device=None):
         self.ladder = side_ladder()
         self.meshes = {}
+        self.device = device
 
     def shape(self, kind, cells):
         if kind == "cavity":
@@ -111,7 +117,7 @@ class MeshCache:
         key = (kind, nx, ny)
         if key not in self.meshes:
             lx = 1.0 if kind == "cavity" else float(CHANNEL_ASPECT)
-            m = Mesh(create_2D_grid((0, 0, 0), nx, ny, lx, 1.0, 0.1))
+            m = Mesh(create_2D_grid((0, 0, 0), nx, ny, lx, 1.0, 0.1), device=self.device)
             define_boundary_walls(m)
             self.meshes[key] = m
         return self.meshes[key]
@@ -147,20 +153,31 @@ def build_solver(req: Request, mesh, atol=1e-8, maxiter=500, device=None, rtol=(
     nu = req.speed * 1.0 / req.re
     model = FVM(mesh, device=device)
     model.material.create_incompressible_newtonian_fluid(viscosity=nu, density=1.0)
-    b = model.boundary
     if req.kind == "cavity":
         model.set_reference_pressure(0, 0.0)
-        b.no_slip_wall("-X")
-        b.no_slip_wall("+X")
-        b.no_slip_wall("-Y")
-        b.velocity_BC("+Y", u=req.speed, v=0.0, w=0.0)
-    else:
-        b.velocity_BC("-X", u=req.speed, v=0.0, w=0.0)
-        b.pressure_BC("+X", p=0.0)
-        b.no_slip_wall("-Y")
-        b.no_slip_wall("+Y")
-    b.slip_wall("-Z")
-    b.slip_wall("+Z")
+    # The boundary table of a kind depends on its mesh alone, its values on the lid/inlet
+    # speed alone (every other value is 0): formed once per (mesh, kind) through the
+    # boundary API at unit speed, then scaled -- the same table the API gives at this
+    # speed, bit for bit, without the helpers' per-call work on every admission.
+    cache = mesh.__dict__.setdefault("_serve_bc_templates", {})
+    if req.kind not in cache:
+        b = model.boundary
+        if req.kind == "cavity":
+            b.no_slip_wall("-X")
+            b.no_slip_wall("+X")
+            b.no_slip_wall("-Y")
+            b.velocity_BC("+Y", u=1.0, v=0.0, w=0.0)
+        else:
+            b.velocity_BC("-X", u=1.0, v=0.0, w=0.0)
+            b.pressure_BC("+X", p=0.0)
+            b.no_slip_wall("-Y")
+            b.no_slip_wall("+Y")
+        b.slip_wall("-Z")
+        b.slip_wall("+Z")
+        cache[req.kind] = (b.boundary_type.copy(), b.boundary_values.copy())
+    btype, bunit = cache[req.kind]
+    model.boundary.boundary_type[...] = btype
+    model.boundary.boundary_values[...] = bunit * float(req.speed)
     model.finalize()
     ur, pr = RELAXATION[req.kind]
     solver = IncompressibleSolver(model, ur * relax_scale, pr * relax_scale)
@@ -286,7 +303,7 @@ class Server:
     def __init__(self, hbm_budget=16 << 30, max_active=256, tol=1e-6, check_every=10, max_outer=4000, patience=5,
                  buckets=(4096, 8192, 16384, 32768, 65536), atol=SERVE_ATOL, rtol=SERVE_RTOL, device=None,
                  clock=time.perf_counter, keep_fields=False, autotune=True, use_graphs=True, max_retries=1,
-                 retry_relax=0.5, p_refine=SERVE_P_REFINE, admission="fifo"):
+                 retry_relax=0.5, p_refine=SERVE_P_REFINE, admission="fifo", admit_slice_s=0.002):
         self.budget = int(hbm_budget)
         self.max_active = int(max_active)
         self.tol = float(tol)
@@ -298,7 +315,7 @@ class Server:
         self.rtol = tuple(rtol)
         self.device = device or torch.device("cuda", torch.cuda.current_device())
         self.clock = clock
-        self.meshes = MeshCache()
+        self.meshes = MeshCache(device=self.device)
         self.autotune = autotune
         self.use_graphs = use_graphs
         # divergence policy: a case whose residual turns non-finite starts again from zero
@@ -312,10 +329,17 @@ class Server:
         if admission not in ("fifo", "largest"):
             raise ValueError("admission must be 'fifo' or 'largest'")
         self.admission = admission
+        # admission yields to the bucket loop after this much host time, so a burst of
+        # arrivals does not hold back the next rounds of the buckets already running
+        self.admit_slice_s = float(admit_slice_s)
         self._geometry_charged = set()
         self._geometry_bytes = 0
         self.keep_fields = keep_fields
         self.streams = [torch.cuda.Stream(device=self.device) for _ in self.bounds]
+        # cases are built (allocations, fills, uploads) on a side stream of their own, so
+        # admission does not queue behind or beside the default stream; a bucket's stream
+        # waits for it before its next round
+        self.admit_stream = torch.cuda.Stream(device=self.device)
         # one cluster size per bucket, from its bound, so a case's arithmetic never depends
         # on which other cases share its batch: the fewest CTAs whose shared memory holds
         # the bucket's largest case (2D-extruded hex meshes: off-diagonal width 4), which
@@ -434,7 +458,10 @@ class Server:
             if arrived and self.admission == "largest":
                 # longest first: the large cases start early and small ones fill the tail
                 waiting.sort(key=lambda r: (-r.cells, r.arrival))
+            t_slice = self.clock()
             while waiting:
+                if self.clock() - t_slice > self.admit_slice_s and (any(active) or any(incoming)):
+                    break
                 req = waiting[0]
                 # a request that no state of the server can admit is rejected, not queued
                 # (it would hold the head of the queue for ever)
@@ -449,7 +476,8 @@ class Server:
                     break
                 ta = self.clock()
                 try:
-                    slot = self._admit(req, t0)
+                    with torch.cuda.stream(self.admit_stream):
+                        slot = self._admit(req, t0)
                 except (ValueError, KeyError, AssertionError, NotImplementedError, _lib.WcfdError) as e:
                     report.admit_s += self.clock() - ta
                     report.results.append(Result(req.rid, req.kind, req.cells, 0, False, float("nan"), req.arrival,
@@ -492,7 +520,8 @@ class Server:
                         if (not math.isfinite(r) and s.retries < self.max_retries
                                 and s.iterations < self.max_outer):
                             # diverged: restart from zero fields at reduced relaxation
-                            s2 = self._restart(s, t0)
+                            with torch.cuda.stream(self.admit_stream):
+                                s2 = self._restart(s, t0)
                             used += s2.bytes - s.bytes
                             incoming[bi].append(s2)
                             continue
@@ -522,6 +551,7 @@ class Server:
                     batches[bi] = CaseBatch([s.solver for s in active[bi]], cluster_size=self.cluster_sizes[bi])
                 # the bucket's stream runs after the uploads of admitted cases and the table
                 stream.wait_stream(cur)
+                stream.wait_stream(self.admit_stream)
                 if fresh and self.autotune:
                     from .autotune import tune_field_block
                     with torch.cuda.stream(stream):
@@ -557,7 +587,7 @@ def run_drop_in(requests, tol=1e-6, check_every=10, max_outer=4000, atol=SERVE_A
     order, with the server's stop and divergence policy (a diverged case restarts from
     zero fields at reduced relaxation, at most ``max_retries`` times): the baseline the
     batched server is compared with."""
-    meshes = MeshCache()
+    meshes = MeshCache(device=device if device is not None else torch.device("cuda", torch.cuda.current_device()))
     stop = StopRule(tol, patience)
     cell_iters = 0
     t0 = time.perf_counter()
