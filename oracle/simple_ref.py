@@ -29,17 +29,23 @@ gradient zeroes every field's gradient (model.py:237); rUA uses the relaxed u-ro
 diagonal for all three components (solver_kernels.py:14-16); term scale is assigned,
 not multiplied (terms.py:92-113).
 
-Parity status: PARITY UNPINNED against the reference's own outputs.  The reference
-runs only on NVIDIA Warp (warp-lang, not vendored, pinned warp==1.0.4 at
-requirements.txt:9) which is absent here and on the GPU machine, and the reference ships
-no test vectors.  The Krylov arithmetic (warp.optim.linear cg / bicgstab with the
-diagonal preconditioner, warp.sparse SpMV) lives in that package; this file restates
-the published preconditioned CG and right-preconditioned BiCGSTAB with an explicit
-stop test ``||r||_2 <= atol`` checked before every iteration, ``maxiter`` = 500 and
-atol = 1e-5 (fp32) / 1e-6 (fp64) as at FV/terms/equation.py:35-39.  What is pinned:
-the mesh pass against a loop restatement (mesh_ref.py), the discrete operators
-against analytic known answers, and the converged cavity against the Ghia et al.
-centre-line tables the reference ships (examples/LDC/*.txt|csv).
+Parity status: PINNED against the reference's own outputs.  The reference runs only on
+NVIDIA Warp (warp-lang, not vendored, pinned warp==1.0.4 at requirements.txt:9), which is
+not installed on these machines; tests/golden/make_reference_golden.py runs the unmodified
+warp_cfd sources on a numpy stand-in for Warp (oracle/warp_stand_in) in float64 with
+tightened Krylov solves, and this restatement, fed the reference's own mesh arrays,
+reproduces those fields to <= 5e-11 (tests/test_reference_pin.py: steady cavity, channel,
+skew-corrected and non-orthogonally corrected jittered cavities, PISO).  The Krylov
+arithmetic of the reference (warp.optim.linear cg / bicgstab with the diagonal
+preconditioner, warp.sparse SpMV) lives in warp-lang; this file restates the published
+preconditioned CG and right-preconditioned BiCGSTAB with an explicit stop test
+``||r||_2 <= atol`` checked before every iteration, ``maxiter`` = 500 and atol = 1e-5
+(fp32) / 1e-6 (fp64) as at FV/terms/equation.py:35-39, so at the reference's own loose stop
+the two may end a solve at different iterations; with the solves tightened they agree.
+Also pinned: the mesh pass against a loop restatement (mesh_ref.py) and the reference's
+own mesh arrays, the discrete operators against analytic known answers, and the converged
+cavity against the Ghia et al. centre-line tables the reference ships
+(examples/LDC/*.txt|csv).
 """
 from __future__ import annotations
 
