@@ -542,7 +542,12 @@ def run_ours(args):
            "d2h_bytes_per_step": C * 16, "same_steps_as_timed": same}
 
     # roofline of the dominant kernel (algorithmic bytes / event time)
-    cg_bytes = sum(perfmodel.cg_bytes(C, W, int(k)) for k in k_p)
+    from warpcfd_gb300 import _lib
+    rows = int(_lib.load().wcfd_batch_max_rows(W))  # rows per CTA of the cluster-resident CG
+    grid_cg = C > 16 * rows
+    # the grid CG streams int16 column offsets when the mesh has them (wcfd_mesh.ell_dcol)
+    col_bytes = 2 if grid_cg and g.get("ell_dcol") is not None else 4
+    cg_bytes = sum(perfmodel.cg_bytes(C, W, int(k), col_bytes) for k in k_p)
     bi_bytes = sum(perfmodel.bicgstab_bytes(C, W, int(k)) for k in k_u)
     peaks = {}
     try:
@@ -551,9 +556,7 @@ def run_ours(args):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     if cg_ms.sum() >= bicg_ms.sum():
-        from warpcfd_gb300 import _lib
-        rows = int(_lib.load().wcfd_batch_max_rows(W))  # rows per CTA of the cluster-resident CG
-        kname = "cg_cluster_kernel" if C <= 16 * rows else "cg_kernel"
+        kname = "cg_kernel" if grid_cg else "cg_cluster_kernel"
         kbytes, kms, nl = cg_bytes, cg_ms.sum(), K_
     else:
         kname, kbytes, kms, nl = "bicgstab_kernel", bi_bytes, bicg_ms.sum(), K_
@@ -562,7 +565,8 @@ def run_ours(args):
     mt = MEASURED_TRAFFIC.get(args.workload)
     if mt is not None and kname.startswith("cg"):
         traffic = mt["per_launch"] + mt["per_iteration"] * float(k_p.mean())
-    step_bytes = [perfmodel.simple_step_bytes(C, K, Ki, B, F, W, int(a), int(b))["total"] for a, b in zip(k_u, k_p)]
+    step_bytes = [perfmodel.simple_step_bytes(C, K, Ki, B, F, W, int(a), int(b), col_bytes=col_bytes)["total"]
+                  for a, b in zip(k_u, k_p)]
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K_, "warmup": args.warmup,
         "ms_per_step": total_ms / K_, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

@@ -73,6 +73,10 @@ typedef struct wcfd_mesh {
     const float*   face_dvec;     /* [K*4] owner->neighbour centroid vector d (internal faces)
                                      and 0; read only by the opt-in explicit internal terms
                                      (wcfd_params.explicit_terms), may be NULL otherwise */
+    const int16_t* ell_dcol;      /* [W*C] ell_col - row as int16, when every |ell_col - row|
+                                     <= 32767 (e.g. a structured numbering), else NULL: the
+                                     grid-cooperative CG then streams 2 bytes per slot
+                                     instead of 4 (the same columns, the same bits) */
 } wcfd_mesh;
 
 /* boundary tables, one row per boundary face, columns u,v,w,p */

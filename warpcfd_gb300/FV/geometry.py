@@ -33,6 +33,17 @@ import numpy as np
 NULL_SLOT = np.int32(-2**31)  # the face reference of a null slot (kNullSlot in the kernels)
 
 
+def ell_offsets(ell_col):
+    """The ELL columns (slot-major, (W, C)) as int16 offsets from their row when every
+    |column - row| fits (a structured or bandwidth-ordered numbering), else None: the grid
+    Krylov kernels then stream 2 bytes per slot instead of 4 (wcfd_mesh.ell_dcol)."""
+    C = ell_col.shape[1]
+    if C == 0:
+        return None
+    d = ell_col.astype(np.int64) - np.arange(C, dtype=np.int64)[None, :]
+    return d.astype(np.int16) if int(np.abs(d).max()) <= 32767 else None
+
+
 def build_geometry(mesh, correction: bool = False) -> dict:
     fp, cp, g = mesh.face_properties, mesh.cell_properties, mesh._geometry64
     f4 = np.float32
@@ -97,6 +108,7 @@ def build_geometry(mesh, correction: bool = False) -> dict:
     pos = (np.cumsum(m, axis=1) - 1)
     cc, ff = np.nonzero(m)
     ell_col[pos[cc, ff], cc] = nbr[cc, ff]
+    ell_dcol = ell_offsets(ell_col) if W > 0 else None
 
     return dict(
         n_cells=C, n_faces=K, n_bfaces=len(bids), faces_per_cell=F, ell_width=W,
@@ -104,4 +116,5 @@ def build_geometry(mesh, correction: bool = False) -> dict:
         face_interp=face_interp, face_normal=face_normal, face_gdiff=gdiff.astype(np.float32),
         face_rpf=rpf.astype(np.float32), cell_slot=cell_slot, cell_volume=vol.astype(np.float32),
         ell_col=ell_col.astype(np.int32), boundary_face=bids.astype(np.int32), face_dvec=face_dvec,
+        ell_dcol=ell_dcol,
     )

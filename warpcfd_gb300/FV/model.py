@@ -144,7 +144,8 @@ class FVM:
             g["face_owner"].data_ptr(), g["face_nbr"].data_ptr(), g["face_brow"].data_ptr(),
             g["face_interp"].data_ptr(), g["face_normal"].data_ptr(), gdiff.data_ptr(),
             g["face_rpf"].data_ptr(), g["cell_slot"].data_ptr(), g["cell_volume"].data_ptr(),
-            g["ell_col"].data_ptr(), g["boundary_face"].data_ptr(), g["face_dvec"].data_ptr())
+            g["ell_col"].data_ptr(), g["boundary_face"].data_ptr(), g["face_dvec"].data_ptr(),
+            g["ell_dcol"].data_ptr() if g.get("ell_dcol") is not None else None)
 
     def bc_struct(self) -> _lib.BC_t:
         return _lib.BC_t(self.boundary_type.data_ptr(), self.boundary_value.data_ptr())

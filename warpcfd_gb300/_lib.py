@@ -44,7 +44,8 @@ class Mesh_t(ct.Structure):
                 ("faces_per_cell", ct.c_int32), ("ell_width", ct.c_int32), ("pad_", ct.c_int32),
                 ("face_owner", vp), ("face_nbr", vp), ("face_brow", vp), ("face_interp", vp),
                 ("face_normal", vp), ("face_gdiff", vp), ("face_rpf", vp), ("cell_slot", vp),
-                ("cell_volume", vp), ("ell_col", vp), ("boundary_face", vp), ("face_dvec", vp)]
+                ("cell_volume", vp), ("ell_col", vp), ("boundary_face", vp), ("face_dvec", vp),
+                ("ell_dcol", vp)]
 
 
 class BC_t(ct.Structure):

@@ -79,6 +79,34 @@ int coop_capacity(const void* fn, int /*unused*/) {
     return cap;
 }
 
+// Grid of a persistent kBlock-thread kernel over n items: every block resident at once
+// (blocks per SM from the occupancy query, cached per kernel and device), fewer when
+// there are fewer items than resident threads.
+int resident_grid(const void* fn, long long n) {
+    static std::mutex mu;
+    struct Entry { const void* fn; int dev; int cap; };
+    static Entry cache[16];
+    static int nc = 0;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int cap = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        for (int i = 0; i < nc; ++i)
+            if (cache[i].fn == fn && cache[i].dev == dev) cap = cache[i].cap;
+        if (cap == 0) {
+            int per_sm = 0, sms = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kBlock, 0);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            cap = per_sm * sms;
+            if (cap < 1) cap = 1;
+            if (nc < 16) cache[nc++] = Entry{fn, dev, cap};
+        }
+    }
+    const int want = grid_for(n);
+    return want < cap ? (want < 1 ? 1 : want) : cap;
+}
+
 int launch_krylov(const void* fn, int slot, const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws ws,
                   double atol, int maxiter, wcfd_solve_stats* stats, cudaStream_t st, const char* name,
                   double rtol = 0.0) {
@@ -305,9 +333,11 @@ int wcfd_face_pass_flags(const wcfd_mesh* m, wcfd_bc bc, wcfd_state s, uint32_t 
                !s.mass_fluxes,
            WCFD_ERR_ARGUMENT, "null field");
     if (mask == WCFD_ALL)
-        face_pass_kernel<<<grid_for(m->n_faces), kBlock, 0, S(stream)>>>(*m, bc, s, mask, flags & 15u, nullptr);
+        face_pass_kernel<<<resident_grid((const void*)face_pass_kernel, m->n_faces), kBlock, 0, S(stream)>>>(
+            *m, bc, s, mask, flags & 15u, nullptr);
     else
-        face_pass_partial_kernel<<<grid_for(m->n_faces), kBlock, 0, S(stream)>>>(*m, bc, s, mask, flags & 15u, nullptr);
+        face_pass_partial_kernel<<<resident_grid((const void*)face_pass_partial_kernel, m->n_faces), kBlock, 0, S(stream)>>>(
+            *m, bc, s, mask, flags & 15u, nullptr);
     LAUNCH_CHECK("face_pass_kernel");
     return WCFD_OK;
 }
@@ -353,7 +383,7 @@ int wcfd_cell_to_face(const wcfd_mesh* m, const float* cell, float* face, void* 
     int rc = check_mesh(m);
     if (rc) return rc;
     RET_IF(!cell || !face, WCFD_ERR_ARGUMENT, "null array");
-    cell_to_face_kernel<<<grid_for(m->n_faces), kBlock, 0, S(stream)>>>(*m, cell, face);
+    cell_to_face_kernel<<<resident_grid((const void*)cell_to_face_kernel, m->n_faces), kBlock, 0, S(stream)>>>(*m, cell, face);
     LAUNCH_CHECK("cell_to_face_kernel");
     return WCFD_OK;
 }
@@ -527,7 +557,7 @@ static int cg_solve(const wcfd_mesh* m, wcfd_system A, float* x, wcfd_krylov_ws 
     RET_IF(maxiter < 0 || !(atol >= 0.0) || !(rtol >= 0.0), WCFD_ERR_ARGUMENT, "bad tolerance or maxiter");
     rc = try_cluster_cg(m, A, x, atol, maxiter, stats, S(stream), rtol);
     if (rc >= 0) return rc;
-    return launch_krylov(cg_kernel_for(m->ell_width), 0, m, A, x, ws, atol, maxiter, stats, S(stream), "cg_kernel",
+    return launch_krylov(cg_kernel_for(m->ell_width, m->ell_dcol != nullptr), 0, m, A, x, ws, atol, maxiter, stats, S(stream), "cg_kernel",
                          rtol);
 }
 
@@ -601,9 +631,13 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
     NvtxRange step_range(c.prm.steady ? "wcfd SIMPLE iteration" : "wcfd PISO step");
     const wcfd_mesh& m = c.mesh;
     const uint32_t skew = c.prm.skew ? 4u : 0u;
-    const int gf = grid_for(m.n_faces), gc = grid_for(m.n_cells);
+    const int gc = grid_for(m.n_cells);
+    // the face kernels are persistent: resident blocks striding over the faces
+    const int gfa = resident_grid((const void*)face_pass_kernel, m.n_faces);
+    const int gfp = resident_grid((const void*)face_pass_partial_kernel, m.n_faces);
+    const int gfc = resident_grid((const void*)cell_to_face_kernel, m.n_faces);
     // incompressible.py:96-99
-    face_pass_kernel<<<gf, kBlock, 0, st>>>(m, c.bc, c.state, WCFD_ALL, 1u | 2u | skew | (c.prm.rhie_chow ? 16u : 0u),
+    face_pass_kernel<<<gfa, kBlock, 0, st>>>(m, c.bc, c.state, WCFD_ALL, 1u | 2u | skew | (c.prm.rhie_chow ? 16u : 0u),
                                             c.rua_faces);
     LAUNCH_CHECK("face_pass_kernel");
     gradient_kernel<<<gc, kBlock, 0, st>>>(m, c.state, WCFD_ALL, nullptr, CorrectArgs{nullptr, nullptr});
@@ -624,13 +658,13 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
     // :118-123
     hbya_kernel<<<gc, kBlock, 0, st>>>(m.n_cells, c.state.cell_gradients, c.rua, c.hbya, c.state.cell_values);
     LAUNCH_CHECK("hbya_kernel");
-    cell_to_face_kernel<<<gf, kBlock, 0, st>>>(m, c.rua, c.rua_faces);
+    cell_to_face_kernel<<<gfc, kBlock, 0, st>>>(m, c.rua, c.rua_faces);
     LAUNCH_CHECK("cell_to_face_kernel");
     for (int inner = 0; inner < c.prm.n_inner; ++inner) {
         NvtxRange r("wcfd pressure corrector");
         for (int ortho = 0; ortho < c.prm.n_ortho; ++ortho) {
             // :127-132
-            face_pass_kernel<<<gf, kBlock, 0, st>>>(m, c.bc, c.state, WCFD_ALL, 2u | skew, nullptr);
+            face_pass_kernel<<<gfa, kBlock, 0, st>>>(m, c.bc, c.state, WCFD_ALL, 2u | skew, nullptr);
             LAUNCH_CHECK("face_pass_kernel");
             gradient_kernel<<<gc, kBlock, 0, st>>>(m, c.state, WCFD_ALL, c.div, CorrectArgs{nullptr, nullptr});
             LAUNCH_CHECK("gradient_kernel");
@@ -647,11 +681,11 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
             if (rc) return rc;
             if (last) mark(3);
             // :144-147
-            p_update_kernel<<<gc, kBlock, 0, st>>>(m.n_cells, c.p_x, c.state.cell_values,
+            p_update_kernel<<<grid_for(m.n_cells, 4 * kBlock), kBlock, 0, st>>>(m.n_cells, c.p_x, c.state.cell_values,
                                                    c.prm.steady ? c.prm.p_relax : 0.0f);
             LAUNCH_CHECK("p_update_kernel");
             // :150-156
-            face_pass_partial_kernel<<<gf, kBlock, 0, st>>>(m, c.bc, c.state, WCFD_P, skew, nullptr);
+            face_pass_partial_kernel<<<gfp, kBlock, 0, st>>>(m, c.bc, c.state, WCFD_P, skew, nullptr);
             LAUNCH_CHECK("face_pass_partial_kernel");
             gradient_kernel<<<gc, kBlock, 0, st>>>(m, c.state, WCFD_P, nullptr, CorrectArgs{c.hbya, c.rua});
             LAUNCH_CHECK("gradient_kernel");
@@ -740,5 +774,5 @@ extern "C" int wcfd_cg_noalloc(const wcfd_mesh* m, wcfd_system A, float* x, doub
     ws.partials = reinterpret_cast<double*>(b + kNoAllocPartialsOff);
     ws.results = nullptr;
     ws.barrier = reinterpret_cast<uint32_t*>(b + kNoAllocBarrierOff);
-    return launch_krylov(cg_kernel_for(m->ell_width), 0, m, A, x, ws, atol, maxiter, stats, S(stream), "cg_kernel");
+    return launch_krylov(cg_kernel_for(m->ell_width, m->ell_dcol != nullptr), 0, m, A, x, ws, atol, maxiter, stats, S(stream), "cg_kernel");
 }

@@ -24,18 +24,34 @@ namespace wcfd {
 //        written with the full owner-to-neighbour distance); rua_f may be null otherwise.
 // kAll: 1 when the caller knows mask == WCFD_ALL, 0 when it knows it is not (the code for
 // the whole-record path is then left out, and with it its registers), -1 to test at run time.
+// The face's own records ([K] arrays) do not depend on the cell ids: they are issued
+// with the ids, so a face is two global-memory round trips deep (ids and records, then
+// the cells).  The persistent kernels below issue the next face's records before the
+// current face's cell loads, so the two round trips of consecutive faces overlap.
+struct FaceRec {
+    int P, N;
+    float4 gi, nrm;
+};
+
+__device__ __forceinline__ FaceRec load_face_rec(const wcfd_mesh& m, uint32_t flags, int k) {
+    FaceRec r;
+    r.P = __ldg(m.face_owner + k);
+    r.N = __ldg(m.face_nbr + k);
+    r.gi = __ldg(reinterpret_cast<const float4*>(m.face_interp) + k);
+    r.nrm = (flags & 2u) ? __ldg(reinterpret_cast<const float4*>(m.face_normal) + k)
+                         : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    return r;
+}
+
 template <int kAll = -1>
-__device__ __forceinline__ void face_pass_body(const wcfd_mesh& m, const wcfd_bc& bc, const wcfd_state& s, uint32_t mask_in, uint32_t flags, int k,
-                                               const float* __restrict__ rua_f = nullptr) {
+__device__ __forceinline__ void face_pass_rec(const wcfd_mesh& m, const wcfd_bc& bc, const wcfd_state& s, uint32_t mask_in, uint32_t flags, int k,
+                                              const FaceRec& rec, const float* __restrict__ rua_f = nullptr) {
     const uint32_t mask = kAll == 1 ? (uint32_t)WCFD_ALL : mask_in;
     const bool all = kAll < 0 ? mask == WCFD_ALL : kAll == 1;
-    const int P = __ldg(m.face_owner + k);
-    const int N = __ldg(m.face_nbr + k);
-    // the face's own records ([K] arrays) do not depend on the cell ids: issued with them,
-    // so a face is two global-memory round trips deep (ids and records, then the cells)
-    const float4 gi = __ldg(reinterpret_cast<const float4*>(m.face_interp) + k);
-    const float4 nrm = (flags & 2u) ? __ldg(reinterpret_cast<const float4*>(m.face_normal) + k)
-                                    : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const int P = rec.P;
+    const int N = rec.N;
+    const float4 gi = rec.gi;
+    const float4 nrm = rec.nrm;
     // an internal face with every field selected overwrites all four values: no read
     float4 fv = (N >= 0 && all) ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : ld4(s.face_values + 4 * (size_t)k);
     const float4 cp = ld4(s.cell_values + 4 * (size_t)P);
@@ -112,22 +128,53 @@ __device__ __forceinline__ void face_pass_body(const wcfd_mesh& m, const wcfd_bc
     }
 }
 
-__global__ void __launch_bounds__(kBlock) face_pass_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s,
+template <int kAll = -1>
+__device__ __forceinline__ void face_pass_body(const wcfd_mesh& m, const wcfd_bc& bc, const wcfd_state& s, uint32_t mask, uint32_t flags, int k,
+                                               const float* __restrict__ rua_f = nullptr) {
+    face_pass_rec<kAll>(m, bc, s, mask, flags, k, load_face_rec(m, flags, k), rua_f);
+}
+
+// Persistent form: a grid of resident blocks strides over the faces; each thread issues
+// the next face's ids and records, then completes the current face.
+template <int kAll>
+__device__ __forceinline__ void face_pass_loop(const wcfd_mesh& m, const wcfd_bc& bc, const wcfd_state& s, uint32_t mask,
+                                               uint32_t flags, const float* rua_f) {
+    const int K = m.n_faces;
+    const int stride = gridDim.x * kBlock;
+    int k = blockIdx.x * kBlock + threadIdx.x;
+    if (k >= K) return;
+    FaceRec cur = load_face_rec(m, flags, k);
+    for (;;) {
+        const bool more = k < K - stride;
+        FaceRec nxt;
+        if (more) nxt = load_face_rec(m, flags, k + stride);
+        face_pass_rec<kAll>(m, bc, s, mask, flags, k, cur, rua_f);
+        if (!more) break;
+        k += stride;
+        cur = nxt;
+    }
+}
+
+// blocks per SM the all-field pass is compiled for (registers: 65,536 / (256 x this))
+#ifndef WCFD_FACE_PASS_MINB
+#define WCFD_FACE_PASS_MINB 3
+#endif
+#ifndef WCFD_FACE_PARTIAL_MINB
+#define WCFD_FACE_PARTIAL_MINB 5
+#endif
+
+__global__ void __launch_bounds__(kBlock, WCFD_FACE_PASS_MINB) face_pass_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s,
                                                            uint32_t mask, uint32_t flags, const float* rua_f) {
-    const int k = blockIdx.x * kBlock + threadIdx.x;
-    if (k >= m.n_faces) return;
     // launched with mask == WCFD_ALL only; the run-time test compiles to faster code here
     // than the compile-time form (measured on the 128^3 cavity: 118.9 against 134.6 us)
-    face_pass_body(m, bc, s, mask, flags, k, rua_f);
+    face_pass_loop<-1>(m, bc, s, mask, flags, rua_f);
 }
 
 // the same pass for a mask other than WCFD_ALL (the pressure-only pass of the correction
 // loop): per-field loads only, fewer registers, more warps in flight
-__global__ void __launch_bounds__(kBlock, 6) face_pass_partial_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s,
+__global__ void __launch_bounds__(kBlock, WCFD_FACE_PARTIAL_MINB) face_pass_partial_kernel(wcfd_mesh m, wcfd_bc bc, wcfd_state s,
                                                                    uint32_t mask, uint32_t flags, const float* rua_f) {
-    const int k = blockIdx.x * kBlock + threadIdx.x;
-    if (k >= m.n_faces) return;
-    face_pass_body<0>(m, bc, s, mask, flags, k, rua_f);
+    face_pass_loop<0>(m, bc, s, mask, flags, rua_f);
 }
 
 // Green-Gauss gradient (model.py:232-239, model_kernels.py:71-90):
@@ -242,11 +289,31 @@ __device__ __forceinline__ void cell_to_face_body(const wcfd_mesh& m, const floa
     }
 }
 
+// persistent, the next face's ids and weight issued before the current face's cell loads
 __global__ void __launch_bounds__(kBlock) cell_to_face_kernel(wcfd_mesh m, const float* __restrict__ x,
                                                               float* __restrict__ y) {
-    const int k = blockIdx.x * kBlock + threadIdx.x;
-    if (k >= m.n_faces) return;
-    cell_to_face_body(m, x, y, k);
+    const int K = m.n_faces;
+    const int stride = gridDim.x * kBlock;
+    int k = blockIdx.x * kBlock + threadIdx.x;
+    if (k >= K) return;
+    int P = __ldg(m.face_owner + k), N = __ldg(m.face_nbr + k);
+    float psi = __ldg(m.face_interp + 4 * (size_t)k + 3);
+    for (;;) {
+        const bool more = k < K - stride;
+        int Pn = 0, Nn = 0;
+        float psin = 0.0f;
+        if (more) {
+            Pn = __ldg(m.face_owner + k + stride);
+            Nn = __ldg(m.face_nbr + k + stride);
+            psin = __ldg(m.face_interp + 4 * (size_t)(k + stride) + 3);
+        }
+        y[k] = N < 0 ? x[P] : psi * x[P] + (1.0f - psi) * x[N];
+        if (!more) break;
+        k += stride;
+        P = Pn;
+        N = Nn;
+        psi = psin;
+    }
 }
 
 // After the momentum solve (incompressible.py:118-123):
@@ -299,11 +366,27 @@ __device__ __forceinline__ void p_update_body(int C, const float* __restrict__ p
     else *p = p_new[c];
 }
 
+// four cells per thread, every load issued before the first store (p_update_body's
+// arithmetic): the kernel writes 4 bytes of each 16-byte cell row, so its sectors are
+// read anyway and the pass is bound by how many of them are in flight
 __global__ void __launch_bounds__(kBlock) p_update_kernel(int C, const float* __restrict__ p_new,
                                                           float* __restrict__ cell_values, float alpha) {
-    const int c = blockIdx.x * kBlock + threadIdx.x;
-    if (c >= C) return;
-    p_update_body(C, p_new, cell_values, alpha, c);
+    constexpr int kU = 4;
+    const int c0 = blockIdx.x * kBlock * kU + threadIdx.x;
+    float pn[kU], po[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+        const int c = c0 + u * kBlock;
+        if (c < C) {
+            pn[u] = p_new[c];
+            po[u] = alpha > 0.0f ? cell_values[4 * (size_t)c + 3] : 0.0f;
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+        const int c = c0 + u * kBlock;
+        if (c < C) cell_values[4 * (size_t)c + 3] = alpha > 0.0f ? alpha * pn[u] + (1.0f - alpha) * po[u] : pn[u];
+    }
 }
 
 }  // namespace wcfd

@@ -73,7 +73,8 @@ struct KrylovArgs {
     wcfd_solve_stats* stats;
 };
 // kernel instantiations for off-diagonal width W (0..6), nullptr otherwise
-const void* cg_kernel_for(int W);
+// delta: read the columns from wcfd_mesh.ell_dcol (int16 offsets from the row)
+const void* cg_kernel_for(int W, bool delta);
 const void* barrier_check_kernel_ptr();
 const void* bicgstab_kernel_for(int W);
 const void* cg_cluster_kernel_for(int W, int R);

@@ -74,6 +74,43 @@ __device__ void write_stats(const KrylovArgs& a, const KScalars& sc) {
     }
 }
 
+// L2 prefetch of the matrix lines that a warp's rows use `ahead` grid-stride trips of one
+// row later: lane l < 2 W takes slab l (columns, then coefficients) and prefetches the
+// lines of the warp's first and last row there (one line when the 32 rows are 128-byte
+// aligned).  Nothing waits on a prefetch and no register is held.  Used by the BiCGSTAB,
+// whose vectors (nine 3C arrays) exceed L2 anyway, where it takes a DRAM round trip out of
+// each trip of the SpMV passes (0.374 -> 0.338 ms per 128^3 momentum solve).  The grid CG
+// keeps its vectors in L2 and reads the matrix evict-first; every prefetch variant tried
+// there (per line at normal priority, or a bulk prefetch of each block's 4 KB slabs with
+// the evict-first policy, 1 to 5 trips ahead) made its iteration slower (35.4 us ->
+// 41-47 us on 128^3).
+template <int W>
+__device__ __forceinline__ void prefetch_matrix_lines(const int* col, const float* off, int C, int stride, int i,
+                                                      int ahead) {
+    if constexpr (W > 0) {
+        const int lane = threadIdx.x & 31;
+        if (lane < 2 * W) {
+            const long long rb = (long long)i - lane + (long long)ahead * stride;
+            if (rb < C) {
+                const long long rl = rb + 31 < C ? rb + 31 : C - 1;
+                const char* base = lane < W ? reinterpret_cast<const char*>(col + (size_t)lane * C)
+                                            : reinterpret_cast<const char*>(off + (size_t)(lane - W) * C);
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(base + (size_t)rb * 4));
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(base + (size_t)rl * 4));
+            }
+        }
+    }
+}
+
+// Column of slot j of row i: from the int16 offsets (kD, wcfd_mesh.ell_dcol) or the int32
+// columns, streamed (evict-first) or with a plain load.
+template <bool kD, bool kStream>
+__device__ __forceinline__ int ell_column(const int* __restrict__ col, const int16_t* __restrict__ dcol, size_t idx,
+                                          int i) {
+    if constexpr (kD) return i + (int)(kStream ? __ldcs(dcol + idx) : dcol[idx]);
+    else return kStream ? __ldcs(col + idx) : col[idx];
+}
+
 // Jacobi-preconditioned CG on a scalar system, W = off-diagonal width known at compile
 // time so the loads of a row's columns and gathered values are all in flight at once.
 // Workspace: r, pA, pB, q, invd, z (6 C floats).
@@ -89,7 +126,13 @@ __device__ void write_stats(const KrylovArgs& a, const KScalars& sc) {
 // thread takes two rows (i, i + stride) per trip of pass (1) so that twice the column,
 // coefficient and gather loads are in flight: the pass is bound by memory latency, not
 // by bandwidth, at one row per thread.
-template <int W>
+//
+// kD: the columns come from the int16 offsets (wcfd_mesh.ell_dcol) instead of the int32
+// columns, 6 W instead of 8 W streamed bytes per row (the same columns, the same bits):
+// pass (1) streams the matrix from DRAM while the vectors stay in L2, so on the 128^3
+// cavity (W = 6) an iteration went from 35.5 to 33.3 us.  The BiCGSTAB keeps the int32
+// columns: the offsets made its solve slower there (0.338 -> 0.360 ms).
+template <int W, bool kD>
 __global__ void __launch_bounds__(BS, 1) cg_kernel(KrylovArgs a) {
     __shared__ KScalars sc;
     const int C = a.m.n_cells;
@@ -102,6 +145,7 @@ __global__ void __launch_bounds__(BS, 1) cg_kernel(KrylovArgs a) {
     const float* __restrict__ diag = a.A.diag;
     const float* __restrict__ off = a.A.off;
     const int* __restrict__ col = a.m.ell_col;
+    const int16_t* __restrict__ dcol = a.m.ell_dcol;
     float* x = a.x;
     const int stride = gridDim.x * BS;
     const int i0 = blockIdx.x * BS + threadIdx.x;
@@ -116,7 +160,7 @@ __global__ void __launch_bounds__(BS, 1) cg_kernel(KrylovArgs a) {
     for (int i = i0; i < C; i += stride) {
         float ax = diag[i] * x[i];
 #pragma unroll
-        for (int j = 0; j < W; ++j) ax += off[(size_t)j * C + i] * x[col[(size_t)j * C + i]];
+        for (int j = 0; j < W; ++j) ax += off[(size_t)j * C + i] * x[ell_column<kD, false>(col, dcol, (size_t)j * C + i, i)];
         const float ri = b[i] - ax;
         const float di = jacobi(diag[i]);
         const float zi = ri * di;
@@ -155,8 +199,8 @@ __global__ void __launch_bounds__(BS, 1) cg_kernel(KrylovArgs a) {
             float o1[WA], o2[WA];
 #pragma unroll
             for (int j = 0; j < W; ++j) {
-                c1[j] = __ldcs(col + (size_t)j * C + i);
-                c2[j] = __ldcs(col + (size_t)j * C + k2);
+                c1[j] = ell_column<kD, true>(col, dcol, (size_t)j * C + i, i);
+                c2[j] = ell_column<kD, true>(col, dcol, (size_t)j * C + k2, k2);
             }
 #pragma unroll
             for (int j = 0; j < W; ++j) {
@@ -308,6 +352,7 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
         // p = r + beta (p - omega v) ; v = A (M p) ; r0.v
         ff accv[1] = {ff_zero()};
         for (int i = i0; i < C; i += stride) {
+            prefetch_matrix_lines<W>(col, off, C, stride, i, 1);
             float pi[3], vi[3];
 #pragma unroll
             for (int o = 0; o < 3; ++o) {
@@ -351,6 +396,7 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
         // s = r - alpha v ; x += alpha M p ; t = A (M s) ; t.t ; t.s
         ff acct[2] = {ff_zero(), ff_zero()};
         for (int i = i0; i < C; i += stride) {
+            prefetch_matrix_lines<W>(col, off, C, stride, i, 1);
             float si[3], ti[3];
 #pragma unroll
             for (int o = 0; o < 3; ++o) {
@@ -387,18 +433,29 @@ __global__ void __launch_bounds__(BS) bicgstab_kernel(KrylovArgs a) {
         }
         __syncthreads();
         const float of = sc.of;
-        // x += omega M s ; r = s - omega t ; r.r ; r0.r
+        // x += omega M s ; r = s - omega t ; r.r ; r0.r -- every load of the row issued
+        // before its first store (x and r may alias the others as far as the compiler
+        // knows), components accumulated in order
         ff accr[2] = {ff_zero(), ff_zero()};
         for (int i = i0; i < C; i += stride) {
+            float sv[3], dv[3], xv[3], tv[3], rv0[3];
 #pragma unroll
             for (int o = 0; o < 3; ++o) {
                 const size_t q = 3 * (size_t)i + o;
-                const float si = s[q];
-                x[q] += of * (si * invd[q]);
-                const float ri = si - of * t[q];
+                sv[o] = s[q];
+                dv[o] = invd[q];
+                xv[o] = x[q];
+                tv[o] = t[q];
+                rv0[o] = r0[q];
+            }
+#pragma unroll
+            for (int o = 0; o < 3; ++o) {
+                const size_t q = 3 * (size_t)i + o;
+                x[q] = xv[o] + of * (sv[o] * dv[o]);
+                const float ri = sv[o] - of * tv[o];
                 r[q] = ri;
                 ff_fma(accr[0], ri, ri);
-                ff_fma(accr[1], r0[q], ri);
+                ff_fma(accr[1], rv0[o], ri);
             }
         }
         ff rr2[2];
@@ -490,15 +547,17 @@ __global__ void __launch_bounds__(BS, 1) barrier_check_kernel(GridCtl g, int ski
 
 const void* barrier_check_kernel_ptr() { return (const void*)barrier_check_kernel; }
 
-const void* cg_kernel_for(int W) {
+// W = 0 has no columns to read: its offset form is the plain one
+template <bool kD>
+const void* cg_kernel_pick(int W) {
     switch (W) {
-        case 0: return (const void*)cg_kernel<0>;
-        case 1: return (const void*)cg_kernel<1>;
-        case 2: return (const void*)cg_kernel<2>;
-        case 3: return (const void*)cg_kernel<3>;
-        case 4: return (const void*)cg_kernel<4>;
-        case 5: return (const void*)cg_kernel<5>;
-        case 6: return (const void*)cg_kernel<6>;
+        case 0: return (const void*)cg_kernel<0, false>;
+        case 1: return (const void*)cg_kernel<1, kD>;
+        case 2: return (const void*)cg_kernel<2, kD>;
+        case 3: return (const void*)cg_kernel<3, kD>;
+        case 4: return (const void*)cg_kernel<4, kD>;
+        case 5: return (const void*)cg_kernel<5, kD>;
+        case 6: return (const void*)cg_kernel<6, kD>;
         default: return nullptr;
     }
 }
@@ -515,5 +574,7 @@ const void* bicgstab_kernel_for(int W) {
         default: return nullptr;
     }
 }
+
+const void* cg_kernel_for(int W, bool delta) { return delta ? cg_kernel_pick<true>(W) : cg_kernel_pick<false>(W); }
 
 }  // namespace wcfd

@@ -475,7 +475,8 @@ int blocks_for(long long n, int bs) { return (int)((n + bs - 1) / bs); }
 //   [1] boundary row of a boundary face outside [0, B)
 //   [2] a cell slot that is not null and names a face outside [0, K)
 //   [3] a cell slot whose face does not have this cell on the side the slot says
-//   [4] an off-diagonal column outside [0, C)
+//   [4] an off-diagonal column outside [0, C), or (with ell_dcol) an offset that does not
+//       give the column
 constexpr int kChecks = 5;
 
 __global__ void check_faces_kernel(wcfd_mesh m, int* __restrict__ bad) {
@@ -506,6 +507,7 @@ __global__ void check_cells_kernel(wcfd_mesh m, int* __restrict__ bad) {
     for (int j = 0; j < m.ell_width; ++j) {
         const int col = m.ell_col[(size_t)j * m.n_cells + c];
         if (col < 0 || col >= m.n_cells) atomicAdd(bad + 4, 1);
+        else if (m.ell_dcol && c + (int)m.ell_dcol[(size_t)j * m.n_cells + c] != col) atomicAdd(bad + 4, 1);
     }
 }
 

@@ -8,22 +8,23 @@ B boundary), F slots per cell, W off-diagonal width, k Krylov iterations.
 from __future__ import annotations
 
 
-def cg_bytes_per_iteration(C: int, W: int) -> int:
+def cg_bytes_per_iteration(C: int, W: int, col_bytes: int = 4) -> int:
     """One CG iteration (two passes) per row:
     p = z + beta p_old ; q = A p ; x += alpha_prev p_old :
-                   off 4W + col 4W + diag 4 + z 4 + p_old 4 + x 8 (rw) + p 4 (w) + q 4 (w)
+                   off 4W + col (col_bytes) W + diag 4 + z 4 + p_old 4 + x 8 (rw) + p 4 (w) + q 4 (w)
     r -= alpha q ; z = M r : r 8 (rw) + q 4 + invd 4 + z 4 (w)
+    col_bytes 2 when the columns are read as int16 offsets (wcfd_mesh.ell_dcol).
     """
-    return C * (8 * W + 28 + 20)
+    return C * ((4 + col_bytes) * W + 28 + 20)
 
 
-def cg_bytes_setup(C: int, W: int) -> int:
-    """r = b - A x, invd, z, p: off/col 8W, diag 4, x 4, b 4, writes r, invd, z, p 16."""
-    return C * (8 * W + 28)
+def cg_bytes_setup(C: int, W: int, col_bytes: int = 4) -> int:
+    """r = b - A x, invd, z, p: off/col (4 + col_bytes) W, diag 4, x 4, b 4, writes r, invd, z, p 16."""
+    return C * ((4 + col_bytes) * W + 28)
 
 
-def cg_bytes(C: int, W: int, iters: int) -> int:
-    return cg_bytes_setup(C, W) + iters * cg_bytes_per_iteration(C, W)
+def cg_bytes(C: int, W: int, iters: int, col_bytes: int = 4) -> int:
+    return cg_bytes_setup(C, W, col_bytes) + iters * cg_bytes_per_iteration(C, W, col_bytes)
 
 
 def bicgstab_bytes_per_iteration(C: int, W: int) -> int:
@@ -74,7 +75,7 @@ def pressure_assembly_bytes(C: int, K: int, F: int, W: int, B: int) -> int:
     return 16 * F * C + 4 * K + 4 * K + 4 * K + B * (4 + 1 + 8) + 4 * W * C + 8 * C + 4 * C
 
 
-def simple_step_bytes(C, K, Ki, B, F, W, k_u, k_p, n_corr=1) -> dict:
+def simple_step_bytes(C, K, Ki, B, F, W, k_u, k_p, n_corr=1, col_bytes=4) -> dict:
     d = {
         "face_pass": face_pass_bytes(C, K, Ki, B) * 2 * n_corr + face_pass_bytes(C, K, Ki, B, mdot=False) * n_corr,
         "gradient": gradient_bytes(C, K, F) + gradient_bytes(C, K, F, div=True) * n_corr
@@ -82,7 +83,7 @@ def simple_step_bytes(C, K, Ki, B, F, W, k_u, k_p, n_corr=1) -> dict:
         "momentum_assemble": momentum_assembly_bytes(C, K, F, W, B),
         "pressure_assemble": pressure_assembly_bytes(C, K, F, W, B) * n_corr,
         "bicgstab": bicgstab_bytes(C, W, k_u),
-        "cg": cg_bytes(C, W, k_p) * n_corr,
+        "cg": cg_bytes(C, W, k_p, col_bytes) * n_corr,
         "small": 32 * C + 12 * K,
     }
     d["total"] = sum(d.values())

@@ -222,9 +222,9 @@ def estimate_bytes(cells: int) -> int:
 
 def estimate_geometry_bytes(cells: int) -> int:
     """Admission estimate of a mesh's device geometry before it is built: a 2D-extruded hex
-    mesh has about four faces per cell (68 B of face records each), six 16-byte cell slots
-    and four 4-byte off-diagonal columns per cell, about 390 B per cell; 420 B per cell plus
-    64 KiB stays above geometry_bytes() on the mix's meshes."""
+    mesh has about four faces per cell (68 B of face records each), six 16-byte cell slots,
+    four 4-byte off-diagonal columns and their four 2-byte offsets per cell, about 400 B per
+    cell; 420 B per cell plus 64 KiB stays above geometry_bytes() on the mix's meshes."""
     return int(420 * cells + 64 * 1024)
 
 
