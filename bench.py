@@ -44,8 +44,9 @@ WORKLOADS = {
                 "solve (3 sweeps, inner relative stop 1e-3); one step = one time step",
     "serve": "serving mix: steady cavity/channel requests, cells log-uniform in [32^2, 256^2], Re ~ U[50, 1000], "
              "speed ~ U[0.5, 2], seeded Poisson arrivals, converged: relative momentum residual below 1e-6 and "
-             "no longer falling (no new minimum over 5 checks of 10 iterations); "
-             "continuous batching (batched form) vs the drop-in path one case at a time",
+             "no longer falling (no new minimum over 10 checks of 10 iterations); "
+             "continuous batching (batched form; its pressure CG in the single-reduction arrangement) vs the "
+             "drop-in path one case at a time (textbook CG)",
 }
 METRIC = "cell-iterations/s"
 
@@ -53,11 +54,11 @@ METRIC = "cell-iterations/s"
 # (`dram__bytes_read.sum + dram__bytes_write.sum`, one capture per workload):
 #   channel   cg_cluster_kernel: 1.47 MB per launch whatever the iteration count (the
 #             system is read once into shared memory)
-#   cavity3d  cg_kernel: 21.08 GB for a 174-iteration launch = 121.2 MB per iteration
-#             (the vectors stay in L2; the matrix streams)
+#   cavity3d  cg_kernel (int16 column offsets): 15.40 GB for a 174-iteration launch =
+#             88.5 MB per iteration (the vectors stay in L2; the matrix streams)
 MEASURED_TRAFFIC = {
     "channel": {"per_launch": 1.473e6, "per_iteration": 0.0},
-    "cavity3d": {"per_launch": 0.0, "per_iteration": 20.24e9 / 174},
+    "cavity3d": {"per_launch": 0.0, "per_iteration": 15.403e9 / 174},
 }
 
 
@@ -383,13 +384,13 @@ def serve_mix(args, local, rank=0, world=1, dist=None):
     reqs_all = make_request_mix(args.requests, seed=0, rate=args.rate)
     reqs = shard(reqs_all, rank, world)
     # warm-up: a few small requests touch every kernel and the caches
-    Server(max_outer=30).run(make_request_mix(4, seed=1, rate=1e6, lo=32 * 32, hi=48 * 48))
+    Server(max_outer=30, cg_variant=args.serve_cg).run(make_request_mix(4, seed=1, rate=1e6, lo=32 * 32, hi=48 * 48))
     torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
     with ClockSampler(local, enabled=not args.no_clocks) as clocks:
         rep = Server(max_outer=args.max_outer, max_active=args.max_active, use_graphs=args.serve_graphs,
-                     admission=args.admission).run(reqs)
+                     admission=args.admission, cg_variant=args.serve_cg).run(reqs)
     summ = rep.summary()
     wall = max_over_ranks(summ["wall_s"])
     cell_its = sum_over_ranks(rep.cell_iterations)
@@ -407,6 +408,7 @@ def serve_mix(args, local, rank=0, world=1, dist=None):
     drop_status["retried"] = int(sum(res[3] > 0 for res in drop["results"]))
     return {
         "value": value, "wall": wall, "requests": len(reqs_all), "serving": summ, "clocks": clocks.summary(),
+        "batched_pressure_cg": "single-reduction" if args.serve_cg == 1 else "textbook",
         "drop_in": {"requests_per_rank": len(sample), "sample": "stratified: evenly spaced over the mix sorted by "
                     "(kind, cells)", "sample_kinds": by_kind, "mix_kinds": mix_kind,
                     "sample_cells_median": float(np.median([r.cells for r in sample])),
@@ -633,6 +635,8 @@ def main():
     ap.add_argument("--drop-in-sample", type=int, default=48, help="serve workload: requests run through the drop-in")
     ap.add_argument("--admission", default="fifo", choices=["fifo", "largest"],
                     help="serve workload: admission order of arrived requests")
+    ap.add_argument("--serve-cg", type=int, default=1, help="serving: the batched pressure CG, 0 textbook, "
+                    "1 single-reduction (one cluster all-reduce per iteration; the server's default)")
     ap.add_argument("--serve-graphs", type=int, default=1, help="serve workload: replay each bucket round as a "
                     "captured CUDA graph (1) or launch it eagerly (0)")
     args = ap.parse_args()

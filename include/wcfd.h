@@ -398,6 +398,10 @@ typedef struct wcfd_batch_dims {
                                 solve (each: residual in fp64 from p_x64, a correction CG to
                                 the case's p_refine_rtol, p_x64 += correction); 0 = the
                                 plain solve.  Every case then needs p_x64 and p_work. */
+    int32_t cg_variant;      /* 0 = textbook Jacobi CG (the reference's arithmetic); 1 = the
+                                single-reduction (Chronopoulos-Gear) arrangement: one cluster
+                                all-reduce and one cluster barrier per iteration instead of two
+                                all-reduces, the same iterates up to rounding */
 } wcfd_batch_dims;
 
 /* Cluster size wcfd_batch_simple_iteration would pick for these dims (0 = no cluster

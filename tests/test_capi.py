@@ -42,9 +42,9 @@ def test_struct_layout_matches_header(tmp_path):
                     'sizeof(wcfd_state), sizeof(wcfd_system), sizeof(wcfd_krylov_ws), sizeof(wcfd_solve_stats), '
                     'sizeof(wcfd_params), sizeof(wcfd_case), offsetof(wcfd_case, prm), offsetof(wcfd_case, stats), '
                     'sizeof(wcfd_mesh_cells), sizeof(wcfd_mesh_faces), offsetof(wcfd_mesh_faces, node_width), '
-                    'sizeof(wcfd_batch_dims)); printf("%zu %zu %zu %zu %zu\\n", sizeof(wcfd_term_fields), '
+                    'sizeof(wcfd_batch_dims)); printf("%zu %zu %zu %zu %zu %zu %zu\\n", sizeof(wcfd_term_fields), '
                     'sizeof(wcfd_term), offsetof(wcfd_term, scale), offsetof(wcfd_batch_dims, p_refine), '
-                    '(size_t)WCFD_MAX_TERMS);}\n')
+                    '(size_t)WCFD_MAX_TERMS, offsetof(wcfd_mesh, ell_dcol), offsetof(wcfd_batch_dims, cg_variant));}\n')
     exe = tmp_path / "layout"
     subprocess.run(["gcc", f"-I{os.path.join(ROOT, 'include')}", str(prog), "-o", str(exe)], check=True)
     got = list(map(int, subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()))
@@ -53,7 +53,8 @@ def test_struct_layout_matches_header(tmp_path):
     want += [_lib.Case_t.prm.offset, _lib.Case_t.stats.offset, ct.sizeof(_lib.MeshCells_t),
              ct.sizeof(_lib.MeshFaces_t), _lib.MeshFaces_t.node_width.offset, ct.sizeof(_lib.BatchDims_t)]
     want += [ct.sizeof(_lib.TermFields_t), ct.sizeof(_lib.Term_t), _lib.Term_t.scale.offset,
-             _lib.BatchDims_t.p_refine.offset, _lib.MAX_TERMS]
+             _lib.BatchDims_t.p_refine.offset, _lib.MAX_TERMS, _lib.Mesh_t.ell_dcol.offset,
+             _lib.BatchDims_t.cg_variant.offset]
     assert got == want
 
 

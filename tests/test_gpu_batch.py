@@ -189,3 +189,46 @@ def test_batch_rejects_mixed_refinement_counts():
     s1.p_refine = 1
     with pytest.raises(ValueError, match="refinement"):
         CaseBatch([s0, s1])
+
+
+@pytest.mark.parametrize("cluster_size", [1, 4])
+def test_single_reduction_cg_tracks_textbook(cluster_size):
+    """The batched single-reduction CG (wcfd_batch_dims.cg_variant = 1: one cluster
+    all-reduce and one cluster barrier per iteration) follows the textbook batched CG
+    within the step tolerances, with 1, 2 and 4 rows per thread (a 64^2 cavity on one CTA
+    holds 4,096 rows) and, on 4-CTA clusters, neighbours in other CTAs; a case in the mix
+    equals the same case alone bitwise."""
+    from warpcfd_gb300.batch import CaseBatch
+
+    def cases():
+        out = []
+        for mk, bc, ref, nu in ((lambda: cavity_mesh(16), cavity_bc, 0, 0.01),
+                                (lambda: channel_mesh(80, 16), channel_bc, None, 0.05),
+                                (lambda: cavity_mesh(64), cavity_bc, 0, 0.01)):
+            model, solver, _ = make_pair(mk(), bc, ref_cell=ref, nu=nu, atol=1e-7)
+            out.append((model, solver))
+        return out
+
+    steps = 4
+    runs = {}
+    for variant in (0, 1):
+        mix = cases()
+        batch = CaseBatch([s for _, s in mix], cluster_size=cluster_size, cg_variant=variant)
+        assert batch.dims.cg_variant == variant
+        for _ in range(steps):
+            batch.step()
+        runs[variant] = ([fields(m) for m, _ in mix], batch.solve_stats())
+    got, st1 = runs[1]
+    ref, st0 = runs[0]
+    for i in range(3):
+        assert np.isfinite(got[i]).all(), i
+        for o in range(3):
+            assert vel_err(got[i], ref[i], o) < 1e-4, (i, o)
+        assert rel_l2(got[i][:, 3], ref[i][:, 3]) < 1e-3, i
+        k0, k1 = int(st0[i, 1]["iterations"]), int(st1[i, 1]["iterations"])
+        assert abs(k1 - k0) <= max(2, k0 // 20), (i, k0, k1)
+    model, solver = cases()[2]
+    alone = CaseBatch([solver], cluster_size=cluster_size, cg_variant=1)
+    for _ in range(steps):
+        alone.step()
+    assert np.array_equal(fields(model), got[2])

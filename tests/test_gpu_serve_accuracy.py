@@ -6,9 +6,12 @@ server's own stop (relative momentum residual below 1e-6 and no longer falling, 
 solves to a tenfold drop, the pressure accumulated in fp64 by one refinement sweep per
 outer iteration) and each served field is compared with the fp64 oracle's fixed point of
 the same case (tests/golden/make_golden.py serve_fp64_converged): u, v, w on the velocity
-scale and p relative, within 1e-5 -- or, where float32 arithmetic cannot get that close,
-within three times the fp32 oracle's own distance from that fixed point (the fixture's
-r{i}_fp32; measured: the channel's p, ~2e-5).
+scale and p relative.  The server's default (the batched pressure CG in its
+single-reduction arrangement, stop after 10 checks without a new residual minimum) is held
+to 1e-5 on every field (measured: p 4.0e-6, 7.1e-6, 9.3e-6).  The textbook batched CG is
+held to 1e-5 or, where it stops farther along the fp32 noise floor, three times the fp32
+oracle's own distance from the fixed point (the fixture's r{i}_fp32; measured: p 2.1e-5
+on the 51^2 cavity and 7.3e-5 on the channel, whose fp32 floor is 2.8e-5).
 """
 import os
 
@@ -28,15 +31,17 @@ def _lib_ready():
     build_library()
 
 
-def test_served_results_match_the_fp64_oracle():
-    from warpcfd_gb300.serve import Request, Server
+# cg_variant 0: the textbook batched pressure CG; 1: its single-reduction arrangement
+@pytest.mark.parametrize("cg_variant", [0, 1])
+def test_served_results_match_the_fp64_oracle(cg_variant):
+    from warpcfd_gb300.serve import SERVE_CG_VARIANT, Request, Server
 
     fx = np.load(os.path.join(GOLDEN, "serve_fp64_converged.npz"))
     reqs = []
     for key in sorted(k for k in fx.files if k.endswith("_spec")):
         rid, cells, re, speed, is_cavity = fx[key]
         reqs.append(Request(int(rid), "cavity" if is_cavity else "channel", int(cells), float(re), float(speed), 0.0))
-    rep = Server(keep_fields=True, max_outer=8000).run(reqs)
+    rep = Server(keep_fields=True, max_outer=8000, cg_variant=cg_variant).run(reqs)
     assert len(rep.results) == len(reqs)
     errs = {}
     for r in sorted(rep.results, key=lambda r: r.rid):
@@ -55,4 +60,5 @@ def test_served_results_match_the_fp64_oracle():
         errs[r.rid] = (e, floor)
     for rid, (e, floor) in errs.items():
         for f in "uvwp":
-            assert e[f] <= max(1e-5, 3.0 * floor[f]), (rid, f, e, floor)
+            bound = 1e-5 if cg_variant == SERVE_CG_VARIANT else max(1e-5, 3.0 * floor[f])
+            assert e[f] <= bound, (rid, f, e, floor)

@@ -90,7 +90,7 @@ class BatchDims_t(ct.Structure):
     _fields_ = [("max_cells", ct.c_int32), ("max_faces", ct.c_int32), ("faces_per_cell", ct.c_int32),
                 ("ell_width", ct.c_int32), ("n_inner", ct.c_int32), ("n_ortho", ct.c_int32),
                 ("cluster_size", ct.c_int32), ("field_block", ct.c_int32), ("explicit_terms", ct.c_int32),
-                ("p_refine", ct.c_int32)]
+                ("p_refine", ct.c_int32), ("cg_variant", ct.c_int32)]
 
 
 class TermFields_t(ct.Structure):

@@ -24,7 +24,7 @@ class CaseBatch:
     construction (and at refresh()); a caller that steps the batch on another stream must
     first make that stream wait for this one."""
 
-    def __init__(self, solvers, cluster_size: int = 0, device=None, field_block: int = 0):
+    def __init__(self, solvers, cluster_size: int = 0, device=None, field_block: int = 0, cg_variant: int = 0):
         if not solvers:
             raise ValueError("a batch needs at least one case")
         self.solvers = list(solvers)
@@ -47,7 +47,7 @@ class CaseBatch:
             max(s.model.num_cells for s in self.solvers), max(s.model.num_faces for s in self.solvers),
             self.faces_per_cell, self.ell_width, self.solvers[0].NUM_INNER_LOOPS,
             self.solvers[0].NUM_ORTHOGONAL_CORRECTORS, int(cluster_size), int(field_block), 0,
-            int(self.solvers[0].p_refine))
+            int(self.solvers[0].p_refine), int(cg_variant))
         self._graph = None
         self._graph_steps = 0
         self.table = torch.empty(n * ct.sizeof(_lib.Case_t), dtype=torch.uint8, device=self.device)

@@ -117,6 +117,14 @@ __global__ void __launch_bounds__(kMaxFieldBlock) refine_update_batched(const wc
     c.p_x[i] = (float)v;
 }
 
+// the pressure CG of the batch: textbook (cg_variant 0) or single-reduction (1)
+const void* batch_cg_kernel(const wcfd_batch_dims& d, int R) {
+    return d.cg_variant == 1 ? cg1m_cluster_batched_for(d.ell_width, R) : cg_cluster_batched_for(d.ell_width, R);
+}
+size_t batch_cg_smem(const wcfd_batch_dims& d, int R) {
+    return d.cg_variant == 1 ? cluster_cg1m_smem_bytes(R, d.ell_width) : cluster_cg_smem_bytes(R, d.ell_width);
+}
+
 #define BCHECK(what)                                                                               \
     do {                                                                                           \
         const cudaError_t e_ = cudaGetLastError();                                                 \
@@ -134,12 +142,13 @@ extern "C" int wcfd_batch_prepare(const wcfd_batch_dims* dims) {
     if (!dims || dims->max_cells <= 0 || dims->ell_width < 0 || dims->ell_width > kMaxSlots) return WCFD_ERR_ARGUMENT;
     const int cs = dims->cluster_size > 0 ? dims->cluster_size : pick_cluster(*dims);
     if (cs < 1 || cs > 16) return WCFD_ERR_TOO_LARGE;
+    if (dims->cg_variant != 0 && dims->cg_variant != 1) return WCFD_ERR_ARGUMENT;
     const int R = (dims->max_cells + cs - 1) / cs;
-    const void* cg_fn = cg_cluster_batched_for(dims->ell_width, R);
+    const void* cg_fn = batch_cg_kernel(*dims, R);
     const void* bi_fn = bicgstab_cluster_batched_for(dims->ell_width);
     if (!cg_fn || !bi_fn) return WCFD_ERR_ARGUMENT;
     int rc = prepare_cluster(bi_fn, 0);
-    if (!rc) rc = prepare_cluster(cg_fn, cluster_cg_smem_bytes(R, dims->ell_width));
+    if (!rc) rc = prepare_cluster(cg_fn, batch_cg_smem(*dims, R));
     return rc;
 }
 
@@ -162,7 +171,7 @@ extern "C" int wcfd_batch_simple_iteration(const wcfd_case* cases, int32_t n_cas
     const wcfd_batch_dims d = *dims;
     if (d.max_cells <= 0 || d.max_faces <= 0 || d.faces_per_cell < 1 || d.faces_per_cell > kMaxSlots ||
         d.ell_width < 0 || d.ell_width > d.faces_per_cell || d.n_inner < 0 || d.n_ortho < 0 || n_cases > 65535 ||
-        d.p_refine < 0 || d.p_refine > 64) {
+        d.p_refine < 0 || d.p_refine > 64 || (d.cg_variant != 0 && d.cg_variant != 1)) {
         std::snprintf(g_batch_error, sizeof(g_batch_error), "bad batch dims");
         return WCFD_ERR_ARGUMENT;
     }
@@ -181,7 +190,7 @@ extern "C" int wcfd_batch_simple_iteration(const wcfd_case* cases, int32_t n_cas
         std::snprintf(g_batch_error, sizeof(g_batch_error), "max_cells %d too large for cluster size %d", d.max_cells, cs);
         return WCFD_ERR_TOO_LARGE;
     }
-    const void* cg_fn = cg_cluster_batched_for(d.ell_width, R);
+    const void* cg_fn = batch_cg_kernel(d, R);
     const void* bi_fn = bicgstab_cluster_batched_for(d.ell_width);
     if (!cg_fn || !bi_fn) return WCFD_ERR_ARGUMENT;
     cudaStream_t st = S(stream);
@@ -204,7 +213,7 @@ extern "C" int wcfd_batch_simple_iteration(const wcfd_case* cases, int32_t n_cas
     BCHECK("hbya_batched");
     rua_faces_batched<<<gf, fb, 0, st>>>(cases);
     BCHECK("rua_faces_batched");
-    const size_t smem = cluster_cg_smem_bytes(R, d.ell_width);
+    const size_t smem = batch_cg_smem(d, R);
     for (int inner = 0; inner < d.n_inner; ++inner) {
         for (int ortho = 0; ortho < d.n_ortho; ++ortho) {
             face_pass_batched<<<gf, fb, 0, st>>>(cases, WCFD_ALL, 2u);

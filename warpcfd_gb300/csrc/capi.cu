@@ -681,7 +681,7 @@ int wcfd_simple_iteration(const wcfd_case* cp, void* stream) {
             if (rc) return rc;
             if (last) mark(3);
             // :144-147
-            p_update_kernel<<<grid_for(m.n_cells, 4 * kBlock), kBlock, 0, st>>>(m.n_cells, c.p_x, c.state.cell_values,
+            p_update_kernel<<<gc, kBlock, 0, st>>>(m.n_cells, c.p_x, c.state.cell_values,
                                                    c.prm.steady ? c.prm.p_relax : 0.0f);
             LAUNCH_CHECK("p_update_kernel");
             // :150-156

@@ -366,27 +366,11 @@ __device__ __forceinline__ void p_update_body(int C, const float* __restrict__ p
     else *p = p_new[c];
 }
 
-// four cells per thread, every load issued before the first store (p_update_body's
-// arithmetic): the kernel writes 4 bytes of each 16-byte cell row, so its sectors are
-// read anyway and the pass is bound by how many of them are in flight
 __global__ void __launch_bounds__(kBlock) p_update_kernel(int C, const float* __restrict__ p_new,
                                                           float* __restrict__ cell_values, float alpha) {
-    constexpr int kU = 4;
-    const int c0 = blockIdx.x * kBlock * kU + threadIdx.x;
-    float pn[kU], po[kU];
-#pragma unroll
-    for (int u = 0; u < kU; ++u) {
-        const int c = c0 + u * kBlock;
-        if (c < C) {
-            pn[u] = p_new[c];
-            po[u] = alpha > 0.0f ? cell_values[4 * (size_t)c + 3] : 0.0f;
-        }
-    }
-#pragma unroll
-    for (int u = 0; u < kU; ++u) {
-        const int c = c0 + u * kBlock;
-        if (c < C) cell_values[4 * (size_t)c + 3] = alpha > 0.0f ? alpha * pn[u] + (1.0f - alpha) * po[u] : pn[u];
-    }
+    const int c = blockIdx.x * kBlock + threadIdx.x;
+    if (c >= C) return;
+    p_update_body(C, p_new, cell_values, alpha, c);
 }
 
 }  // namespace wcfd

@@ -85,6 +85,9 @@ int cluster_cg_max_rows(int W, int optin);
 int cluster_cg_rpt(int R);
 const void* cg1_cluster_kernel_for(int W, int R);
 size_t cluster_cg1_smem_bytes(int R, int W);
+// the batched form's single-reduction CG (wcfd_batch_dims.cg_variant = 1), up to 4,096 rows per CTA
+const void* cg1m_cluster_batched_for(int W, int R);
+size_t cluster_cg1m_smem_bytes(int R, int W);
 const void* residual64_kernel_for(int W);
 __global__ void refine_update_kernel(int C, double* x64, const float* d, float* x32);
 __global__ void refine_count_kernel(wcfd_solve_stats* stats, int* acc, int first, int last);

@@ -141,6 +141,15 @@ SERVE_RTOL = (0.1, 0.1)
 # one fp64 refinement sweep of the pressure solve per outer iteration (its correction to the
 # same tenfold drop): the pressure of a converged case is accumulated in fp64
 SERVE_P_REFINE = 1
+# stop rule of a served case: no new residual minimum over this many checks of 10 outer
+# iterations (see StopRule).  Where an fp32 iteration stops along its noise floor sets how
+# close the served fields come to the fp64 fixed point: with 10 checks every field of the
+# accuracy test's requests is within 1e-5 of it (single-reduction CG), with 5 the channel's
+# p stops 8e-5 to 1.2e-4 away.
+SERVE_PATIENCE = 10
+# the batched pressure CG of the server: 1 = single-reduction (wcfd_batch_dims.cg_variant),
+# one cluster all-reduce per iteration instead of two (+11% on the serving mix)
+SERVE_CG_VARIANT = 1
 
 
 def build_solver(req: Request, mesh, atol=1e-8, maxiter=500, device=None, rtol=(0.0, 0.0), relax_scale=1.0,
@@ -236,7 +245,7 @@ class StopRule:
     1e-6 alone is still 3e-5 to 2e-4 from the fp64 fixed point, one run to its floor is
     within ~1e-6 on the velocities and ~1e-5 on p.  patience = 0 stops at ``tol``."""
 
-    def __init__(self, tol=1e-6, patience=5):
+    def __init__(self, tol=1e-6, patience=SERVE_PATIENCE):
         self.tol = float(tol)
         self.patience = int(patience)
 
@@ -300,11 +309,15 @@ class ServeReport:
 class Server:
     """Continuous batching over size buckets (bucket = cell count up to its bound)."""
 
-    def __init__(self, hbm_budget=16 << 30, max_active=256, tol=1e-6, check_every=10, max_outer=4000, patience=5,
+    def __init__(self, hbm_budget=16 << 30, max_active=256, tol=1e-6, check_every=10, max_outer=4000,
+                 patience=SERVE_PATIENCE,
                  buckets=(4096, 8192, 16384, 32768, 65536), atol=SERVE_ATOL, rtol=SERVE_RTOL, device=None,
                  clock=time.perf_counter, keep_fields=False, autotune=True, use_graphs=True, max_retries=1,
-                 retry_relax=0.5, p_refine=SERVE_P_REFINE, admission="fifo", admit_slice_s=0.002):
+                 retry_relax=0.5, p_refine=SERVE_P_REFINE, admission="fifo", admit_slice_s=0.002,
+                 cg_variant=SERVE_CG_VARIANT):
         self.budget = int(hbm_budget)
+        # the batched pressure CG: 0 textbook, 1 single-reduction (wcfd_batch_dims.cg_variant)
+        self.cg_variant = int(cg_variant)
         self.max_active = int(max_active)
         self.tol = float(tol)
         self.stop = StopRule(tol, patience)
@@ -548,7 +561,8 @@ class Server:
                 fresh = batches[bi] is None
                 if fresh:
                     # the case table is uploaded on the current stream
-                    batches[bi] = CaseBatch([s.solver for s in active[bi]], cluster_size=self.cluster_sizes[bi])
+                    batches[bi] = CaseBatch([s.solver for s in active[bi]], cluster_size=self.cluster_sizes[bi],
+                                            cg_variant=self.cg_variant)
                 # the bucket's stream runs after the uploads of admitted cases and the table
                 stream.wait_stream(cur)
                 stream.wait_stream(self.admit_stream)
@@ -582,7 +596,7 @@ class Server:
 
 
 def run_drop_in(requests, tol=1e-6, check_every=10, max_outer=4000, atol=SERVE_ATOL, rtol=SERVE_RTOL, device=None,
-                max_retries=1, retry_relax=0.5, p_refine=SERVE_P_REFINE, patience=5):
+                max_retries=1, retry_relax=0.5, p_refine=SERVE_P_REFINE, patience=SERVE_PATIENCE):
     """The same requests through the plain drop-in path, one case at a time in arrival
     order, with the server's stop and divergence policy (a diverged case restarts from
     zero fields at reduced relaxation, at most ``max_retries`` times): the baseline the
