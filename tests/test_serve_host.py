@@ -172,3 +172,21 @@ def test_boundary_template_times_speed_equals_the_api_table():
         ts, vs = table(m, kind, speed)
         assert np.array_equal(t1, ts)
         assert np.array_equal((v1 * speed).view(np.int64), vs.view(np.int64))
+
+
+def test_server_and_drop_in_share_the_stop_and_solver_policy():
+    """The drop-in baseline runs the server's own stop rule, Krylov stops and refinement
+    sweeps (only the batched pressure CG's arrangement differs), so the two are compared
+    at the same convergence criterion."""
+    import inspect
+
+    from warpcfd_gb300 import serve
+
+    srv = inspect.signature(Server.__init__).parameters
+    drop = inspect.signature(serve.run_drop_in).parameters
+    for name in ("tol", "check_every", "max_outer", "atol", "rtol", "max_retries", "retry_relax", "p_refine",
+                 "patience"):
+        assert srv[name].default == drop[name].default, name
+    assert srv["patience"].default == serve.SERVE_PATIENCE == 10
+    assert srv["cg_variant"].default == serve.SERVE_CG_VARIANT == 1
+    assert inspect.signature(StopRule.__init__).parameters["patience"].default == serve.SERVE_PATIENCE
